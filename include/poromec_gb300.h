@@ -1,0 +1,155 @@
+/*
+ * poromec_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * poroMec per-time-step Biot hot path.
+ *
+ * The reference (lmn-labest/poroMec, Fortran 77/90) has no FFI layer: its
+ * "operator API" is the set of subroutines Main.f calls.  Each entry point
+ * below replaces one of them and keeps its argument meaning; the Fortran
+ * driver binds them with ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Arrays are the Fortran arrays, column-major, leading dimension first:
+ *    ix(nen+1,numel), id(ndf,nnode), x(ndm,nnode), e(PM_PROP,numat),
+ *    u(ndf,nnode).  Node, element, material and equation numbers are
+ *    1-based; ia is int64 and ja int32 as in Datastruct.f.
+ *  - Host pointers are read (or written) only during the call; device state
+ *    lives in the handle.  Entry points with the _dev suffix take device
+ *    pointers and a cudaStream_t (passed as void*).
+ *  - Every call returns a pm_status.  Where the reference stops the program
+ *    (stop_mef, Paralelo.f:1158-1165) the library returns an error instead.
+ *  - One handle per host thread; each handle owns one CUDA stream.
+ */
+#ifndef POROMEC_GB300_H
+#define POROMEC_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PM_PROP 15   /* rows of e(prop,numat); e(1..7) = E, nu, K_h, M, alpha, rho, rho_f */
+#define PM_NFLOAD 6  /* second dimension of fload(maxt, PM_NFLOAD, nloads) */
+
+typedef struct pm_handle_s* pm_handle;
+
+typedef enum {
+  PM_OK = 0,
+  PM_E_ARG = 1,        /* invalid argument or inconsistent sizes */
+  PM_E_DET = 2,        /* Jacobian determinant <= 1e-14 (jacob3d_m, Elmlib.f:2301) */
+  PM_E_ZERO_DIAG = 3,  /* zero diagonal entry (pcg, Iters.f:401-406) */
+  PM_E_NOCONV = 4,     /* Krylov solver reached maxit (Iters.f:499-501) */
+  PM_E_NLNOCONV = 5,   /* nonlinear loop reached maxnlit (Main.f:1046-1053) */
+  PM_E_ELTYPE = 6,     /* element type other than 15 (tetra10) / 17 (hexa20) */
+  PM_E_CUDA = 7,       /* CUDA runtime error (message in pm_last_error) */
+  PM_E_NOMEM = 8,      /* device allocation failed */
+  PM_E_STATE = 9       /* call out of order (e.g. solve before assembly) */
+} pm_status;
+
+typedef struct {
+  int iters;      /* Krylov iterations of the last solve */
+  int nlit;       /* nonlinear iterations of the step */
+  int refine;     /* outer refinement sweeps (mixed precision), else 0 */
+  double conv;    /* tol * ||b||_M of the last solve */
+  double xkx;     /* x.Kx of the last solve (the reference's solver log) */
+  double res_u;   /* last residual norms of cal_residuo_pm */
+  double res_p;
+} pm_step_info;
+
+/* Precision modes (pm_set_precision). */
+#define PM_FP64 0          /* plain FP64: values, vectors and arithmetic */
+#define PM_FP32_REFINE 1   /* FP32 matrix values + FP32-valued inner Krylov
+                              solve inside an FP64 iterative-refinement loop */
+
+/* Mesh set-up: the 'mesh' macro (Main.f:481-870): equation numbering
+ * numeqpmec2 (Numeq.f:86-151), CSRD structure datastruct_pm/csrstruct_pm
+ * (Datastruct.f:1-278, Csr.f:18-307) and element colouring coloredmesh
+ * (Colormsh.f:9-71).
+ *  id:  restraint flags as read by 'constrainpmec' (1 = prescribed, 0 = free)
+ *  fnno: 1 for vertex nodes (pressure dof), 0 for mid-side nodes
+ *  ie:  element type per material: 17 hexa20 (nen 20), 15 tetra10 (nen 10)
+ *  num: node visiting order (reord, Reord.f:1-44), NULL = natural order. */
+int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
+                   int ndf, const int32_t* ix, const int32_t* id,
+                   const int32_t* fnno, const double* x, int numat,
+                   const int32_t* ie, const double* e, const int32_t* num,
+                   pm_handle* out);
+void pm_destroy(pm_handle h);
+const char* pm_last_error(pm_handle h);
+const char* pm_status_string(int status);
+
+/* Loads: eload/eloadp(7,numel) face load ids (elmtloads), nload(ndf,nnode)
+ * nodal time-load ids, f(ndf,nnode) nodal values, load(3,nloads) = type,
+ * number of components, number of time points; fload(maxt,PM_NFLOAD,nloads)
+ * the load tables read by rload (Rdata.f:1487) and evaluated by tload
+ * (Pload.f:220-377).  Any pointer may be NULL (= zero). */
+int pm_set_loads(pm_handle h, const int32_t* eload, const int32_t* eloadp,
+                 const int32_t* nload, const double* f, int nloads, int maxt,
+                 const int32_t* load, const double* fload);
+/* gravity(3), dt, t, istep: the transiente/gravity common blocks. */
+int pm_set_env(pm_handle h, const double* gravity, double dt, double t, int istep);
+/* Nodal state u(ndf,nnode), u0(ndf,nnode), dp(nnode); NULL leaves it unchanged. */
+int pm_set_state(pm_handle h, const double* u, const double* u0, const double* dp);
+int pm_get_state(pm_handle h, double* u, double* u0, double* dp);
+/* Initial stress tx0(6,nnode): bstress0 by the element routine isw = 5
+ * (initial_stress, Pform.f:679), added to b0 every step (Main.f:931-933). */
+int pm_set_initial_stress(pm_handle h, const double* tx0);
+int pm_set_precision(pm_handle h, int mode);
+
+int pm_get_sizes(pm_handle h, int* neq, int64_t* nad, int* numcolors,
+                 int64_t* nnz_panel);
+/* Equation numbers id(ndf,nnode) after numeqpmec2 (0 = no equation). */
+int pm_get_id(pm_handle h, int32_t* id);
+/* CSRD arrays in the reference layout: ia(neq+1) int64, ja(nad) int32,
+ * ad(neq), al(nad) (strict lower triangle by rows).  Any pointer may be NULL. */
+int pm_get_csrd(pm_handle h, int64_t* ia, int32_t* ja, double* ad, double* al);
+
+/* pform_pm (Pform.f:1-429): element loop plus assembly.
+ *  isw 2: element matrix and internal force p = s.u; lhs assembles K
+ *         (ad/al zeroed first), rhs does b -= p.   u = du(ndf,nnode).
+ *  isw 4: body forces, previous-state internal forces and face loads, b -= p.
+ *         u = u(n) (ndf,nnode); dp taken from the handle state.
+ *  b(neq) is read and written (host array). */
+int pm_assemble(pm_handle h, int isw, int lhs, int rhs, const double* u, double* b);
+
+/* matvec_csrc_sym_pm (Matvec.f:1504-1598): y = (D + L + L^T) x with the
+ * assembled matrix.  x, y host arrays of length neq. */
+int pm_spmv(pm_handle h, const double* x, double* y);
+
+/* solv_pm (Solv.f:27-780): solver 1 = PCG (Iters.f:299-595),
+ * 7 = preconditioned MINRES (Iters.f:3987-4305, 10 restarts);
+ * precond 2 = diag 1/ad, 5 = |1/ad| (Precond.f:22-79).  x is set to 0 first
+ * (fnew = .true.).  b, x host arrays of length neq. */
+int pm_solve(pm_handle h, int solver, int precond, const double* b, double* x,
+             double tol, int maxit, pm_step_info* info);
+
+/* One 'solv' macro step (Main.f:876-1123) on the device-resident state:
+ * pload_pm, isw 4 loop, predictor, nonlinear loop (isw 2, residual check
+ * cal_residuo_pm with stop_crit 1/2, solve, delta_update_pm), update_res_v2.
+ * reassemble = 0 keeps K from the previous step (valid for linear elastic
+ * elements with unchanged dt and materials); the reference reassembles. */
+int pm_step(pm_handle h, int maxnlit, double tol, int stop_crit, int solver,
+            int precond, double solvtol, int maxit, int reassemble,
+            pm_step_info* info);
+
+/* Device-pointer variants (cudaStream_t passed as void*; NULL = the handle's
+ * stream).  Vectors are FP64 of length neq in equation order. */
+int pm_spmv_dev(pm_handle h, const double* d_x, double* d_y, void* stream);
+int pm_solve_dev(pm_handle h, int solver, int precond, const double* d_b,
+                 double* d_x, double tol, int maxit, pm_step_info* info,
+                 void* stream);
+/* The reference CSRD layout on the device, standalone (no handle):
+ * y = (D + L + L^T) x for ia(neq+1) int64 1-based, ja(nad) int32 1-based. */
+int pm_matvec_csrd_dev(int neq, const int64_t* d_ia, const int32_t* d_ja,
+                       const double* d_ad, const double* d_al,
+                       const double* d_x, double* d_y, void* stream);
+
+/* Timing of the last pm_step phases in milliseconds (CUDA events):
+ * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,
+ * [3] solve, [4] updates, [5] SpMV kernel time of the solve (sum),
+ * [6] number of SpMV launches in the solve. */
+int pm_get_timers(pm_handle h, double* t, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

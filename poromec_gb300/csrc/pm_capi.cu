@@ -1,0 +1,932 @@
+// pm_capi.cu -- C ABI of the GB300 Biot hot path: handle management, the
+// pform_pm / matvec / solv_pm replacements and the 'solv' macro step driver.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "pm_internal.h"
+
+using pm::Handle;
+
+namespace {
+
+constexpr int kGraphIters = 16;  // Krylov iterations per captured graph
+
+#define PM_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);           \
+      return PM_E_CUDA;                                                      \
+    }                                                                        \
+  } while (0)
+
+#define PM_TRY(call)              \
+  do {                            \
+    int st_ = (call);             \
+    if (st_ != PM_OK) return st_; \
+  } while (0)
+
+__device__ double d_interp(const double* xs, const double* ys, double xi, int n) {
+  if (xi <= xs[0]) return ys[0];
+  if (xi >= xs[n - 1]) return ys[n - 1];
+  for (int i = 0; i < n - 1; ++i) {
+    const double x1 = xs[i], x2 = xs[i + 1], y1 = ys[i], y2 = ys[i + 1];
+    if (xi >= x1 && xi <= x2) return y1 + (y2 - y1) * (xi - x1) / (x2 - x1);
+  }
+  return 0.0;
+}
+
+// Scalar loads of tload (Pload.f:220-377) evaluated at a node.
+__device__ double d_nodal_load(const int32_t* load, const double* fload, int maxt, int nc,
+                               double t, const double* x, double u, double gmod) {
+  const int ty = load[3 * (nc - 1)];
+  const int nparc = load[3 * (nc - 1) + 1];
+  const int nt = load[3 * (nc - 1) + 2];
+  const double* F = fload + (size_t)maxt * PM_NFLOAD * (nc - 1);
+  auto col = [&](int k) { return F + (size_t)maxt * (k - 1); };
+  const double DOISPI = 6.283185307;
+  switch (ty) {
+    case 1: return F[0];
+    case 2: return F[0] + F[1] * t;
+    case 3: return (F[0] - u) * col(2)[0];
+    case 4:
+    case 5: {
+      double c = 0.0;
+      for (int i = 1; i <= nparc; ++i) {
+        const double a = col(i)[0], w = 1.0 / col(i)[1], t0 = col(i)[2];
+        const double ti = fmax(t - t0, 0.0);
+        c += a * (ty == 4 ? sin(DOISPI * w * ti) : cos(DOISPI * w * ti));
+      }
+      return c;
+    }
+    case 39:
+    case 41:
+    case 43: return d_interp(col(1), col(2), t, nt);
+    case 42: {
+      const double a = d_interp(col(1), col(2), t, nt), b = d_interp(col(1), col(3), t, nt);
+      const double w = d_interp(col(1), col(4), t, nt), t0 = d_interp(col(1), col(5), t, nt);
+      return t0 * (b + a * (w - x[2]) * gmod);
+    }
+    default: return 0.0;
+  }
+}
+
+// pload_pm (Pload.f:1-92): nodal loads and prescribed values at t.
+__global__ void k_pload(int nnode, const int32_t* __restrict__ eq, const int32_t* __restrict__ fnno,
+                        const int32_t* __restrict__ nload, double* __restrict__ f,
+                        double* __restrict__ u, double* __restrict__ b0,
+                        const int32_t* __restrict__ load, const double* __restrict__ fload,
+                        int maxt, const double* __restrict__ x, double t, double dt,
+                        double gmod) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    const int nj = fnno[i] == 1 ? 4 : 3;
+    for (int j = 0; j < nj; ++j) {
+      const size_t q = (size_t)4 * i + j;
+      const int nc = nload ? nload[q] : 0;
+      if (nc > 0) f[q] = d_nodal_load(load, fload, maxt, nc, t, x + 3 * i, u[q], gmod);
+      const int k = eq[q];
+      if (k > 0) b0[k - 1] = (j < 3) ? f[q] : -dt * f[q];
+      else u[q] = f[q];
+    }
+  }
+}
+
+// delta_predict_pm (Predict.f:117-158): u = u - u0
+__global__ void k_predict(int nnode, const int32_t* __restrict__ fnno, double* __restrict__ u,
+                          const double* __restrict__ u0) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    const int nj = fnno[i] == 1 ? 4 : 3;
+    for (int j = 0; j < nj; ++j) u[4 * i + j] -= u0[4 * i + j];
+  }
+}
+
+// delta_update_pm (Predict.f:159-215): du += x on free dofs
+__global__ void k_delta_update(int nnode, const int32_t* __restrict__ eq,
+                               const int32_t* __restrict__ fnno, double* __restrict__ u,
+                               const double* __restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    const int nj = fnno[i] == 1 ? 4 : 3;
+    for (int j = 0; j < nj; ++j) {
+      const int k = eq[4 * i + j];
+      if (k > 0) u[4 * i + j] += x[k - 1];
+    }
+  }
+}
+
+// update_res_v2 (Pload.f:483-540): u = u0 + du, u0 = u, dp += du_p
+__global__ void k_update_res(int nnode, const int32_t* __restrict__ fnno, double* __restrict__ u,
+                             double* __restrict__ u0, double* __restrict__ dp) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    for (int j = 0; j < 3; ++j) {
+      const double v = u0[4 * i + j] + u[4 * i + j];
+      u[4 * i + j] = v;
+      u0[4 * i + j] = v;
+    }
+    if (fnno[i] == 1) {
+      dp[i] += u[4 * i + 3];
+      const double v = u0[4 * i + 3] + u[4 * i + 3];
+      u[4 * i + 3] = v;
+      u0[4 * i + 3] = v;
+    }
+  }
+}
+
+int grid_for(int n) {
+  int g = (n + 255) / 256;
+  return std::max(1, std::min(g, 4 * pm::kRedBlocks));
+}
+
+pm::ElemLaunch elem_launch(Handle* h, int c) {
+  pm::ElemLaunch L;
+  L.ix = h->D.ix;
+  L.eq = h->D.eq;
+  L.x = h->D.x;
+  L.mat = h->D.mat;
+  L.slot = h->D.slot + (size_t)h->nen * h->nen * h->color_ptr[c];
+  L.elems = h->D.color_elems + h->color_ptr[c];
+  L.nelem = h->color_ptr[c + 1] - h->color_ptr[c];
+  L.nen = h->nen;
+  L.node_val_off = h->P.node_val_off;
+  L.node_W = h->P.node_W;
+  L.dt = h->dt;
+  L.t = h->t;
+  L.g0 = h->gravity[0];
+  L.g1 = h->gravity[1];
+  L.g2 = h->gravity[2];
+  L.gmod = h->gravity_mod;
+  L.err = h->D.err;
+  return L;
+}
+
+int check_elem_err(Handle* h) {
+  int e = 0;
+  PM_CUDA(cudaMemcpyAsync(&e, h->D.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  if (e) {
+    PM_CUDA(cudaMemsetAsync(h->D.err, 0, sizeof(int), h->stream));
+    h->err = "element Jacobian determinant <= 1e-14";
+    return PM_E_DET;
+  }
+  return PM_OK;
+}
+
+// isw = 2 with lhs: K into the panels (FP64, and FP32 when refining).
+int assemble_K(Handle* h, bool fp32) {
+  if (fp32) {
+    if (!h->P.val32) {
+      PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
+      h->pcg_graph_val = h->minres_graph_val = nullptr;
+    }
+    PM_CUDA(cudaMemsetAsync(h->P.val32, 0, sizeof(float) * (size_t)h->P.nnz, h->stream));
+  } else {
+    PM_CUDA(cudaMemsetAsync(h->P.val, 0, sizeof(double) * (size_t)h->P.nnz, h->stream));
+  }
+  for (int c = 0; c < h->numcolors; ++c)
+    PM_CUDA(pm::launch_assemble_K(elem_launch(h, c), h->hexa, fp32 ? nullptr : h->P.val,
+                                  fp32 ? h->P.val32 : nullptr, h->stream));
+  if (fp32) h->assembled32 = true;
+  else h->assembled = true;
+  h->assembled_dt = h->dt;
+  return PM_OK;
+}
+
+int residual(Handle* h, const double* du, double* b) {
+  for (int c = 0; c < h->numcolors; ++c)
+    PM_CUDA(pm::launch_residual(elem_launch(h, c), h->hexa, du, b, h->stream));
+  return PM_OK;
+}
+
+int rhs4(Handle* h, const double* u, double* b) {
+  for (int c = 0; c < h->numcolors; ++c)
+    PM_CUDA(pm::launch_rhs4(elem_launch(h, c), h->hexa, u, h->D.dp, h->D.eload, h->D.eloadp,
+                            h->D.load, h->D.fload, h->maxt, b, h->stream));
+  return PM_OK;
+}
+
+// Preconditioner of cal_precond (Precond.f:1601-1721) from the FP64 diagonal.
+int build_precond(Handle* h, int precond) {
+  if (precond != 2 && precond != 5) {
+    h->err = "precond must be 2 (diag) or 5 (|diag|)";
+    return PM_E_ARG;
+  }
+  PM_CUDA(pm::panel_diag(h->P.view(), h->P.val, nullptr, h->D.ad, h->stream));
+  PM_CUDA(cudaMemsetAsync(h->D.err, 0, sizeof(int), h->stream));
+  PM_CUDA(pm::precond(h->neq, h->D.ad, h->D.m, precond == 5, h->D.err, h->stream));
+  int z = 0;
+  PM_CUDA(cudaMemcpyAsync(&z, h->D.err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  if (z) {
+    PM_CUDA(cudaMemsetAsync(h->D.err, 0, sizeof(int), h->stream));
+    h->err = "zero diagonal coefficient";
+    return PM_E_ZERO_DIAG;
+  }
+  return PM_OK;
+}
+
+int read_scalars(Handle* h, pm::KrylovScalars* ks) {
+  PM_CUDA(cudaMemcpyAsync(ks, h->D.ks, sizeof(pm::KrylovScalars), cudaMemcpyDeviceToHost,
+                          h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  return PM_OK;
+}
+
+// Captures kGraphIters Krylov iterations into an executable graph.
+template <typename Body>
+int capture(Handle* h, cudaGraphExec_t* exec, Body body) {
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+  }
+  cudaGraph_t g;
+  PM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t be = cudaSuccess;
+  for (int k = 0; k < kGraphIters && be == cudaSuccess; ++k) be = body();
+  cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+  if (be != cudaSuccess || ee != cudaSuccess) {
+    h->err = std::string("graph capture: ") +
+             cudaGetErrorString(be != cudaSuccess ? be : ee);
+    return PM_E_CUDA;
+  }
+  cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) {
+    h->err = std::string("graph instantiate: ") + cudaGetErrorString(ie);
+    return PM_E_CUDA;
+  }
+  return PM_OK;
+}
+
+// One Krylov solve of K x = b on the device (solv_pm, Solv.f:27-780).
+// val32 != nullptr runs the iteration with FP32 matrix values.
+int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, int maxit,
+           const float* val32, pm_step_info* info) {
+  const int n = h->neq;
+  pm::KrylovVecs& V = h->D.kv;
+  const pm::PanelView P = h->P.view();
+  const double* val64 = val32 ? nullptr : h->P.val;
+  pm::KrylovScalars ks{};
+  cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
+  PM_CUDA(cudaEventRecord(e0, h->stream));
+  if (solver == 1) {
+    const void* vkey = val32 ? (const void*)val32 : (const void*)val64;
+    if (!h->pcg_graph || h->pcg_graph_val != vkey) {
+      PM_TRY(capture(h, &h->pcg_graph, [&]() {
+        return pm::pcg_iteration(P, val64, val32, n, h->D.m, V, h->D.ks, h->D.partial,
+                                 h->D.counter, h->stream);
+      }));
+      h->pcg_graph_val = vkey;
+    }
+    PM_CUDA(pm::pcg_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
+                         h->stream));
+    for (;;) {
+      PM_CUDA(cudaGraphLaunch(h->pcg_graph, h->stream));
+      PM_TRY(read_scalars(h, &ks));
+      if (ks.conv_flag) break;
+    }
+    if (ks.conv_flag != 1) {
+      h->err = ks.conv_flag == 3
+                   ? "PCG: breakdown (non-finite recurrence) after " + std::to_string(ks.iter) +
+                         " iterations"
+                   : "PCG: no convergence reached after " + std::to_string(maxit) + " iterations";
+      if (info) info->iters = ks.iter;
+      return PM_E_NOCONV;
+    }
+  } else if (solver == 7) {
+    const void* vkey = val32 ? (const void*)val32 : (const void*)val64;
+    if (!h->minres_graph || h->minres_graph_val != vkey) {
+      PM_TRY(capture(h, &h->minres_graph, [&]() {
+        return pm::minres_iteration(P, val64, val32, n, h->D.m, V, h->D.ks, h->D.partial,
+                                    h->D.counter, h->stream);
+      }));
+      h->minres_graph_val = vkey;
+    }
+    PM_CUDA(cudaMemsetAsync(h->D.ks, 0, sizeof(pm::KrylovScalars), h->stream));
+    PM_CUDA(pm::minres_conv(n, d_b, h->D.m, h->D.ks, tol, h->D.partial, h->D.counter,
+                            h->stream));
+    int nrestart = 10;  // call_minres, Solv.f:1727
+    bool zero_x = true;
+    for (;;) {
+      PM_CUDA(pm::minres_start(P, val64, val32, n, d_b, h->D.m, V, h->D.ks, maxit, zero_x,
+                               h->D.partial, h->D.counter, h->stream));
+      zero_x = false;
+      for (;;) {
+        PM_CUDA(cudaGraphLaunch(h->minres_graph, h->stream));
+        PM_TRY(read_scalars(h, &ks));
+        if (ks.conv_flag) break;
+      }
+      if (ks.conv_flag == 1) break;
+      if (ks.conv_flag == 3) {
+        h->err = "MINRES: breakdown (non-finite recurrence) after " + std::to_string(ks.iter) +
+                 " iterations";
+        return PM_E_NOCONV;
+      }
+      if (nrestart == 0) {
+        h->err = "MINRES: no convergence reached after " + std::to_string(ks.iter) +
+                 " iterations";
+        if (info) info->iters = ks.iter;
+        return PM_E_NOCONV;
+      }
+      --nrestart;
+    }
+  } else {
+    h->err = "solver must be 1 (pcg) or 7 (minres)";
+    return PM_E_ARG;
+  }
+  PM_CUDA(cudaEventRecord(e1, h->stream));
+  // x.Kx of the solver log (one more product with the converged x)
+  PM_CUDA(pm::spmv(P, val64, val32, V.x, V.q, 3, h->D.ks, h->D.partial, h->D.counter,
+                   h->stream));
+  if (d_x != V.x)
+    PM_CUDA(cudaMemcpyAsync(d_x, V.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  PM_TRY(read_scalars(h, &ks));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  h->timers[5] = ms;
+  h->timers[6] = ks.iter;
+  if (info) {
+    info->iters = ks.iter;
+    info->conv = ks.conv;
+    info->xkx = ks.xkx;
+  }
+  return PM_OK;
+}
+
+// FP64 iterative refinement around an FP32-valued Krylov solve:
+// x = 0; repeat r = b - A64 x (FP64), solve A32 dx = r loosely, x += dx
+// until ||r||_M <= tol ||b||_M.  Residuals, dot products, norms and the
+// diagonal stay FP64.
+int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, int maxit,
+           pm_step_info* info) {
+  const int n = h->neq;
+  const pm::PanelView P = h->P.view();
+  double* r = h->D.rr;
+  double* dx = h->D.dx;
+  PM_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, h->stream));
+  PM_CUDA(cudaMemcpyAsync(r, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  double bnorm = -1.0;
+  int total = 0, sweep = 0;
+  for (sweep = 0; sweep < 60; ++sweep) {
+    // ||r||_|M| = sqrt(sum |m_i| r_i^2), a norm also on the indefinite system
+    double rn2 = 0.0;
+    PM_CUDA(pm::wnorm2(n, r, h->D.m, h->D.norms, h->D.partial, h->D.counter, h->stream));
+    PM_CUDA(cudaMemcpyAsync(&rn2, h->D.norms, sizeof(double), cudaMemcpyDeviceToHost,
+                            h->stream));
+    PM_CUDA(cudaStreamSynchronize(h->stream));
+    const double rn = std::sqrt(rn2);
+    if (bnorm < 0) bnorm = rn;
+    if (rn <= tol * bnorm || rn == 0.0) break;
+    pm_step_info in{};
+    // inner tolerance relative to the current residual, never tighter than
+    // needed for the outer target
+    const double itol = std::max(h->inner_tol, 0.5 * tol * bnorm / rn);
+    PM_TRY(krylov(h, solver, r, dx, itol, maxit, h->P.val32, &in));
+    total += in.iters;
+    PM_CUDA(pm::axpy_into(n, d_x, dx, 1.0, h->stream));
+    // r = b - A64 x  (FP64 panels)
+    PM_CUDA(pm::spmv(P, h->P.val, nullptr, d_x, h->D.by, 0, nullptr, nullptr, nullptr,
+                     h->stream));
+    PM_CUDA(pm::vsub(n, r, d_b, h->D.by, h->stream));
+  }
+  if (info) {
+    info->iters = total;
+    info->refine = sweep;
+    info->conv = tol * bnorm;
+  }
+  return PM_OK;
+}
+
+int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x, double tol,
+              int maxit, pm_step_info* info) {
+  if (!h->assembled) {
+    h->err = "solve before assembly";
+    return PM_E_STATE;
+  }
+  PM_TRY(build_precond(h, precond));
+  if (h->precision == PM_FP32_REFINE) {
+    if (!h->assembled32) {
+      if (!h->P.val32) {
+        PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
+      }
+      PM_CUDA(pm::to_f32(h->P.nnz, h->P.val, h->P.val32, h->stream));
+      h->assembled32 = true;
+    }
+    return refine(h, solver, d_b, d_x, tol, maxit, info);
+  }
+  return krylov(h, solver, d_b, d_x, tol, maxit, nullptr, info);
+}
+
+int alloc_state(Handle* h) {
+  const size_t nn = (size_t)4 * h->nnode, n = h->neq;
+  auto A = [&](double** p, size_t m) -> int {
+    if (cudaMalloc((void**)p, sizeof(double) * std::max<size_t>(m, 1)) != cudaSuccess) {
+      h->err = "cudaMalloc failed";
+      return PM_E_NOMEM;
+    }
+    cudaMemset(*p, 0, sizeof(double) * std::max<size_t>(m, 1));
+    return PM_OK;
+  };
+  pm::Dev& D = h->D;
+  PM_TRY(A(&D.u, nn));
+  PM_TRY(A(&D.u0, nn));
+  PM_TRY(A(&D.f, nn));
+  PM_TRY(A(&D.dp, h->nnode));
+  PM_TRY(A(&D.b0, n));
+  PM_TRY(A(&D.b, n));
+  PM_TRY(A(&D.bst0, n));
+  PM_TRY(A(&D.ad, n));
+  PM_TRY(A(&D.m, n));
+  PM_TRY(A(&D.bx, std::max(n, nn)));
+  PM_TRY(A(&D.by, std::max(n, nn)));
+  PM_TRY(A(&D.rr, n));
+  PM_TRY(A(&D.dx, n));
+  PM_TRY(A(&D.xs, n));
+  pm::KrylovVecs& V = D.kv;
+  for (double** p : {&V.x, &V.r, &V.z, &V.p, &V.q, &V.v, &V.v0, &V.w0, &V.w00, &V.z0})
+    PM_TRY(A(p, n));
+  PM_CUDA(cudaMalloc(&D.ks, sizeof(pm::KrylovScalars)));
+  PM_CUDA(cudaMemset(D.ks, 0, sizeof(pm::KrylovScalars)));
+  PM_TRY(A(&D.partial, 4 * (size_t)pm::kRedBlocks));
+  PM_CUDA(cudaMalloc(&D.counter, sizeof(unsigned) * 4));
+  PM_CUDA(cudaMemset(D.counter, 0, sizeof(unsigned) * 4));
+  PM_TRY(A(&D.norms, 4));
+  PM_CUDA(cudaMalloc(&D.err, sizeof(int)));
+  PM_CUDA(cudaMemset(D.err, 0, sizeof(int)));
+  return PM_OK;
+}
+
+void free_all(Handle* h) {
+  pm::Dev& D = h->D;
+  pm::Panels& P = h->P;
+  void* ptrs[] = {D.ix, D.eq, D.x, D.mat, D.slot, D.color_elems, D.eload, D.eloadp, D.nload,
+                  D.load, D.fload, D.dofkind, D.fnno, D.u, D.u0, D.dp, D.f, D.b0, D.b, D.bst0,
+                  D.ad, D.m, D.bx, D.by, D.rr, D.dx, D.xs, D.kv.x, D.kv.r, D.kv.z, D.kv.p, D.kv.q,
+                  D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
+                  D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
+                  P.val32, P.node_val_off, P.node_W};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
+  if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+pm::MatConst mat_const(const double* e, double gmod) {
+  pm::MatConst m;
+  m.pm_d = e[5] * 1.0e-06;
+  m.fluid_d = e[6] * 1.0e-06;
+  const double ym = e[0], ps = e[1];
+  m.perm = e[2] / (m.fluid_d * gmod);
+  m.imod_biot = 1.0 / e[3];
+  m.coef_biot = e[4];
+  const double a1 = 1.0 - ps, a2 = 1.0 - 2.0 * ps, a3 = 1.0 + ps;
+  m.a = (ym * a1) / (a3 * a2);
+  m.b = ps / a1;
+  m.c = 0.5 * (a2 / a1);
+  return m;
+}
+
+int upload_materials(Handle* h) {
+  h->h_mat.resize(h->numat);
+  for (int k = 0; k < h->numat; ++k) h->h_mat[k] = mat_const(&h->h_e[(size_t)PM_PROP * k], h->gravity_mod);
+  if (!h->D.mat) PM_CUDA(cudaMalloc(&h->D.mat, sizeof(pm::MatConst) * h->numat));
+  PM_CUDA(cudaMemcpy(h->D.mat, h->h_mat.data(), sizeof(pm::MatConst) * h->numat,
+                     cudaMemcpyHostToDevice));
+  h->assembled = h->assembled32 = false;
+  return PM_OK;
+}
+
+template <typename T>
+int set_dev_array(Handle* h, T** dst, const T* src, size_t n) {
+  if (!src) {
+    if (*dst) {
+      cudaFree(*dst);
+      *dst = nullptr;
+    }
+    return PM_OK;
+  }
+  if (!*dst) PM_CUDA(cudaMalloc((void**)dst, sizeof(T) * n));
+  PM_CUDA(cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice));
+  return PM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pm_status_string(int s) {
+  switch (s) {
+    case PM_OK: return "ok";
+    case PM_E_ARG: return "invalid argument";
+    case PM_E_DET: return "element Jacobian determinant <= 1e-14";
+    case PM_E_ZERO_DIAG: return "zero diagonal coefficient";
+    case PM_E_NOCONV: return "Krylov solver did not converge";
+    case PM_E_NLNOCONV: return "nonlinear iteration did not converge";
+    case PM_E_ELTYPE: return "unsupported element type";
+    case PM_E_CUDA: return "CUDA error";
+    case PM_E_NOMEM: return "device allocation failed";
+    case PM_E_STATE: return "call out of order";
+    default: return "unknown status";
+  }
+}
+
+const char* pm_last_error(pm_handle hh) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  return h ? h->err.c_str() : "null handle";
+}
+
+int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
+                   const int32_t* ix, const int32_t* id, const int32_t* fnno, const double* x,
+                   int numat, const int32_t* ie, const double* e, const int32_t* num,
+                   pm_handle* out) {
+  if (!out || !ix || !id || !fnno || !x || !ie || !e || nnode <= 0 || numel <= 0 ||
+      numat <= 0 || ndm != 3 || ndf != 4 ||
+      !((nen == 20 && nenv == 8) || (nen == 10 && nenv == 4)))
+    return PM_E_ARG;
+  *out = nullptr;
+  for (int k = 0; k < numat; ++k)
+    if (!((nen == 20 && ie[k] == 17) || (nen == 10 && ie[k] == 15))) return PM_E_ELTYPE;
+  for (int el = 0; el < numel; ++el) {
+    const int ma = ix[(size_t)(nen + 1) * el + nen];
+    if (ma < 1 || ma > numat) return PM_E_ARG;
+  }
+  Handle* h = new (std::nothrow) Handle();
+  if (!h) return PM_E_NOMEM;
+  h->nnode = nnode;
+  h->nnodev = nnodev;
+  h->numel = numel;
+  h->nen = nen;
+  h->nenv = nenv;
+  h->numat = numat;
+  h->hexa = (nen == 20);
+  h->h_e.assign(e, e + (size_t)PM_PROP * numat);
+  h->h_ie.assign(ie, ie + numat);
+  int st = PM_OK;
+  auto fail = [&](int s) {
+    free_all(h);
+    delete h;
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(PM_E_CUDA);
+  for (auto& ev : h->ev)
+    if (cudaEventCreate(&ev) != cudaSuccess) return fail(PM_E_CUDA);
+  if ((st = pm::build_structure(h, ix, id, fnno, x, num)) != PM_OK) return fail(st);
+  if ((st = alloc_state(h)) != PM_OK) return fail(st);
+  if ((st = upload_materials(h)) != PM_OK) return fail(st);
+  *out = reinterpret_cast<pm_handle>(h);
+  return PM_OK;
+}
+
+void pm_destroy(pm_handle hh) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+}
+
+int pm_set_loads(pm_handle hh, const int32_t* eload, const int32_t* eloadp,
+                 const int32_t* nload, const double* f, int nloads, int maxt,
+                 const int32_t* load, const double* fload) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || nloads < 0 || (nloads > 0 && (!load || !fload || maxt < 1))) return PM_E_ARG;
+  PM_TRY(set_dev_array(h, &h->D.eload, eload, (size_t)7 * h->numel));
+  PM_TRY(set_dev_array(h, &h->D.eloadp, eloadp, (size_t)7 * h->numel));
+  PM_TRY(set_dev_array(h, &h->D.nload, nload, (size_t)4 * h->nnode));
+  if (f) PM_CUDA(cudaMemcpy(h->D.f, f, sizeof(double) * 4 * h->nnode, cudaMemcpyHostToDevice));
+  else PM_CUDA(cudaMemset(h->D.f, 0, sizeof(double) * 4 * h->nnode));
+  h->nloads = nloads;
+  h->maxt = maxt > 0 ? maxt : 1;
+  PM_TRY(set_dev_array(h, &h->D.load, nloads ? load : nullptr, (size_t)3 * nloads));
+  PM_TRY(set_dev_array(h, &h->D.fload, nloads ? fload : nullptr,
+                       (size_t)h->maxt * PM_NFLOAD * nloads));
+  return PM_OK;
+}
+
+int pm_set_env(pm_handle hh, const double* gravity, double dt, double t, int istep) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !(dt > 0.0)) return PM_E_ARG;
+  if (gravity) {
+    for (int i = 0; i < 3; ++i) h->gravity[i] = gravity[i];
+    h->gravity_mod = std::sqrt(gravity[0] * gravity[0] + gravity[1] * gravity[1] +
+                               gravity[2] * gravity[2]);
+    PM_TRY(upload_materials(h));
+  }
+  if (dt != h->dt) h->assembled = h->assembled32 = false;
+  h->dt = dt;
+  h->t = t;
+  h->istep = istep;
+  return PM_OK;
+}
+
+int pm_set_state(pm_handle hh, const double* u, const double* u0, const double* dp) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h) return PM_E_ARG;
+  const size_t nn = (size_t)4 * h->nnode;
+  if (u) PM_CUDA(cudaMemcpy(h->D.u, u, sizeof(double) * nn, cudaMemcpyHostToDevice));
+  if (u0) PM_CUDA(cudaMemcpy(h->D.u0, u0, sizeof(double) * nn, cudaMemcpyHostToDevice));
+  if (dp) PM_CUDA(cudaMemcpy(h->D.dp, dp, sizeof(double) * h->nnode, cudaMemcpyHostToDevice));
+  return PM_OK;
+}
+
+int pm_get_state(pm_handle hh, double* u, double* u0, double* dp) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h) return PM_E_ARG;
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  const size_t nn = (size_t)4 * h->nnode;
+  if (u) PM_CUDA(cudaMemcpy(u, h->D.u, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  if (u0) PM_CUDA(cudaMemcpy(u0, h->D.u0, sizeof(double) * nn, cudaMemcpyDeviceToHost));
+  if (dp) PM_CUDA(cudaMemcpy(dp, h->D.dp, sizeof(double) * h->nnode, cudaMemcpyDeviceToHost));
+  return PM_OK;
+}
+
+int pm_set_initial_stress(pm_handle hh, const double* tx0) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !tx0) return PM_E_ARG;
+  double* d_tx0 = nullptr;
+  PM_CUDA(cudaMalloc(&d_tx0, sizeof(double) * 6 * h->nnode));
+  PM_CUDA(cudaMemcpy(d_tx0, tx0, sizeof(double) * 6 * h->nnode, cudaMemcpyHostToDevice));
+  PM_CUDA(cudaMemsetAsync(h->D.bst0, 0, sizeof(double) * h->neq, h->stream));
+  int st = PM_OK;
+  for (int c = 0; c < h->numcolors && st == PM_OK; ++c) {
+    cudaError_t e = pm::launch_stress5(elem_launch(h, c), h->hexa, d_tx0, h->D.bst0, h->stream);
+    if (e != cudaSuccess) {
+      h->err = cudaGetErrorString(e);
+      st = PM_E_CUDA;
+    }
+  }
+  if (st == PM_OK) st = check_elem_err(h);
+  cudaStreamSynchronize(h->stream);
+  cudaFree(d_tx0);
+  if (st == PM_OK) h->fstress0 = true;
+  return st;
+}
+
+int pm_set_precision(pm_handle hh, int mode) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || (mode != PM_FP64 && mode != PM_FP32_REFINE)) return PM_E_ARG;
+  h->precision = mode;
+  return PM_OK;
+}
+
+int pm_get_sizes(pm_handle hh, int* neq, int64_t* nad, int* numcolors, int64_t* nnz_panel) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h) return PM_E_ARG;
+  if (neq) *neq = h->neq;
+  if (nad) *nad = h->nad;
+  if (numcolors) *numcolors = h->numcolors;
+  if (nnz_panel) *nnz_panel = h->P.nnz;
+  return PM_OK;
+}
+
+int pm_get_id(pm_handle hh, int32_t* id) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !id) return PM_E_ARG;
+  std::memcpy(id, h->h_eq.data(), sizeof(int32_t) * h->h_eq.size());
+  return PM_OK;
+}
+
+int pm_get_csrd(pm_handle hh, int64_t* ia, int32_t* ja, double* ad, double* al) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h) return PM_E_ARG;
+  std::vector<double> val;
+  if (ad || al) {
+    if (!h->assembled) {
+      h->err = "matrix not assembled";
+      return PM_E_STATE;
+    }
+    val.resize(h->P.nnz);
+    PM_CUDA(cudaStreamSynchronize(h->stream));
+    PM_CUDA(cudaMemcpy(val.data(), h->P.val, sizeof(double) * h->P.nnz, cudaMemcpyDeviceToHost));
+  }
+  int64_t pos = 0;
+  int row = 0;
+  if (ia) ia[0] = 1;
+  for (int k = 0; k < h->P.nact; ++k) {
+    const int d = h->h_d[k], W = h->h_W[k], low = h->h_low[k];
+    const int64_t vo = h->h_val_off[k], co = h->h_col_off[k];
+    for (int q = 0; q < d; ++q, ++row) {
+      const int len = low + q;
+      for (int c = 0; c < len; ++c) {
+        if (ja) ja[pos + c] = h->h_cols[co + c] + 1;
+        if (al) al[pos + c] = val[vo + (int64_t)q * W + c];
+      }
+      if (ad) ad[row] = val[vo + (int64_t)q * W + low + q];
+      pos += len;
+      if (ia) ia[row + 1] = pos + 1;
+    }
+  }
+  return PM_OK;
+}
+
+int pm_assemble(pm_handle hh, int isw, int lhs, int rhs, const double* u, double* b) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !u || (rhs && !b) || (isw != 2 && isw != 4)) return PM_E_ARG;
+  const size_t nn = (size_t)4 * h->nnode;
+  PM_CUDA(cudaMemcpyAsync(h->D.bx, u, sizeof(double) * nn, cudaMemcpyHostToDevice, h->stream));
+  if (rhs)
+    PM_CUDA(cudaMemcpyAsync(h->D.by, b, sizeof(double) * h->neq, cudaMemcpyHostToDevice,
+                            h->stream));
+  if (isw == 2) {
+    if (lhs) PM_TRY(assemble_K(h, false));
+    if (rhs) PM_TRY(residual(h, h->D.bx, h->D.by));
+  } else if (rhs) {
+    PM_TRY(rhs4(h, h->D.bx, h->D.by));
+  }
+  PM_TRY(check_elem_err(h));
+  if (rhs)
+    PM_CUDA(cudaMemcpyAsync(b, h->D.by, sizeof(double) * h->neq, cudaMemcpyDeviceToHost,
+                            h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  return PM_OK;
+}
+
+int pm_spmv_dev(pm_handle hh, const double* d_x, double* d_y, void* stream) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !d_x || !d_y) return PM_E_ARG;
+  if (!h->assembled) {
+    h->err = "matrix not assembled";
+    return PM_E_STATE;
+  }
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  PM_CUDA(pm::spmv(h->P.view(), h->P.val, nullptr, d_x, d_y, 0, nullptr, nullptr, nullptr, s));
+  return PM_OK;
+}
+
+int pm_spmv(pm_handle hh, const double* x, double* y) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !x || !y) return PM_E_ARG;
+  if (!h->assembled) {
+    h->err = "matrix not assembled";
+    return PM_E_STATE;
+  }
+  PM_CUDA(cudaMemcpyAsync(h->D.bx, x, sizeof(double) * h->neq, cudaMemcpyHostToDevice, h->stream));
+  PM_CUDA(pm::spmv(h->P.view(), h->P.val, nullptr, h->D.bx, h->D.by, 0, nullptr, nullptr,
+                   nullptr, h->stream));
+  PM_CUDA(cudaMemcpyAsync(y, h->D.by, sizeof(double) * h->neq, cudaMemcpyDeviceToHost, h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  return PM_OK;
+}
+
+int pm_solve_dev(pm_handle hh, int solver, int precond, const double* d_b, double* d_x,
+                 double tol, int maxit, pm_step_info* info, void* stream) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !d_b || !d_x || maxit < 1) return PM_E_ARG;
+  if (stream && (cudaStream_t)stream != h->stream) {
+    // order the handle's stream after the caller's
+    PM_CUDA(cudaEventRecord(h->ev[0], (cudaStream_t)stream));
+    PM_CUDA(cudaStreamWaitEvent(h->stream, h->ev[0], 0));
+  }
+  int st = solve_dev(h, solver, precond, d_b, d_x, tol, maxit, info);
+  if (stream && (cudaStream_t)stream != h->stream) {
+    PM_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    PM_CUDA(cudaStreamWaitEvent((cudaStream_t)stream, h->ev[1], 0));
+  }
+  return st;
+}
+
+int pm_solve(pm_handle hh, int solver, int precond, const double* b, double* x, double tol,
+             int maxit, pm_step_info* info) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !b || !x || maxit < 1) return PM_E_ARG;
+  PM_CUDA(cudaMemcpyAsync(h->D.bx, b, sizeof(double) * h->neq, cudaMemcpyHostToDevice, h->stream));
+  PM_TRY(solve_dev(h, solver, precond, h->D.bx, h->D.by, tol, maxit, info));
+  PM_CUDA(cudaMemcpyAsync(x, h->D.by, sizeof(double) * h->neq, cudaMemcpyDeviceToHost, h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  return PM_OK;
+}
+
+int pm_matvec_csrd_dev(int neq, const int64_t* d_ia, const int32_t* d_ja, const double* d_ad,
+                       const double* d_al, const double* d_x, double* d_y, void* stream) {
+  if (neq <= 0 || !d_ia || !d_ja || !d_ad || !d_al || !d_x || !d_y) return PM_E_ARG;
+  cudaError_t e = pm::csrd_spmv(neq, d_ia, d_ja, d_ad, d_al, d_x, d_y, (cudaStream_t)stream);
+  return e == cudaSuccess ? PM_OK : PM_E_CUDA;
+}
+
+int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, int precond,
+            double solvtol, int maxit, int reassemble, pm_step_info* info) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || maxnlit < 1 || maxit < 1) return PM_E_ARG;
+  cudaStream_t s = h->stream;
+  pm::Dev& D = h->D;
+  cudaEvent_t ev[6];
+  for (auto& e : ev) PM_CUDA(cudaEventCreate(&e));
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      for (int i = 0; i < 6; ++i) cudaEventDestroy(e[i]);
+    }
+  } guard{ev};
+  h->istep += 1;
+  h->t = h->t + h->dt;
+  PM_CUDA(cudaEventRecord(ev[0], s));
+  k_pload<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.nload, D.f, D.u, D.b0,
+                                              D.load, D.fload, h->maxt, D.x, h->t, h->dt,
+                                              h->gravity_mod);
+  PM_CUDA(cudaGetLastError());
+  PM_TRY(rhs4(h, D.u, D.b0));
+  if (h->fstress0) PM_CUDA(pm::axpy_into(h->neq, D.b0, D.bst0, 1.0, s));
+  k_predict<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0);
+  PM_CUDA(cudaGetLastError());
+  PM_CUDA(cudaEventRecord(ev[1], s));
+  bool lhs = true;
+  int it = 1;
+  pm_step_info loc{};
+  double t_asm = 0, t_res = 0, t_sol = 0;
+  for (;;) {
+    PM_CUDA(cudaMemcpyAsync(D.b, D.b0, sizeof(double) * h->neq, cudaMemcpyDeviceToDevice, s));
+    PM_CUDA(cudaEventRecord(ev[2], s));
+    const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
+    if (need_K) {
+      PM_TRY(assemble_K(h, false));
+      h->assembled32 = false;
+    }
+    PM_CUDA(cudaEventRecord(ev[3], s));
+    PM_TRY(residual(h, D.u, D.b));
+    PM_CUDA(cudaEventRecord(ev[4], s));
+    PM_TRY(check_elem_err(h));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[2], ev[3]);
+    t_asm += ms;
+    cudaEventElapsedTime(&ms, ev[3], ev[4]);
+    t_res += ms;
+    if (stop_crit == 1 || stop_crit == 2) {
+      PM_CUDA(pm::resnorms(h->neq, D.b, D.dofkind, D.norms, D.partial, D.counter, s));
+      double nr[2];
+      PM_CUDA(cudaMemcpyAsync(nr, D.norms, sizeof(nr), cudaMemcpyDeviceToHost, s));
+      PM_CUDA(cudaStreamSynchronize(s));
+      // cal_residuo_pm (Residuo.f:39-276)
+      if (stop_crit == 1) {
+        const double res = std::sqrt(nr[0] + nr[1]);
+        if (it == 1) h->res0 = res;
+        else if (it == 2) h->res0 = std::max(h->res0, res);
+        loc.res_u = res;
+        if (res / h->res0 < tol) break;
+      } else {
+        const double gresu = std::sqrt(nr[0]), gresp = std::sqrt(nr[1]);
+        if (it == 1) {
+          h->resu0 = gresu;
+          h->resp0 = gresp;
+        } else if (it == 2) {
+          h->resu0 = std::max(h->resu0, gresu);
+          h->resp0 = std::max(h->resp0, gresu);  // the reference compares with gresu here
+        }
+        loc.res_u = gresu;
+        loc.res_p = gresp;
+        int istop = 0;
+        if (gresu / h->resu0 < tol) istop += 1;
+        if (gresp / h->resp0 < tol) istop += 1;
+        if (istop == 2) break;
+      }
+    }
+    PM_CUDA(cudaEventRecord(ev[2], s));
+    pm_step_info si{};
+    PM_TRY(solve_dev(h, solver, precond, D.b, D.xs, solvtol, maxit, &si));
+    PM_CUDA(cudaEventRecord(ev[3], s));
+    loc.iters = si.iters;
+    loc.refine = si.refine;
+    loc.conv = si.conv;
+    loc.xkx = si.xkx;
+    k_delta_update<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.u, D.xs);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(cudaEventSynchronize(ev[3]));
+    cudaEventElapsedTime(&ms, ev[2], ev[3]);
+    t_sol += ms;
+    if (it >= maxnlit) {
+      h->err = "nonlinear iteration: no convergence after " + std::to_string(it) + " iterations";
+      return PM_E_NLNOCONV;
+    }
+    ++it;
+    lhs = false;
+  }
+  loc.nlit = it;
+  PM_CUDA(cudaEventRecord(ev[5], s));
+  k_update_res<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0, D.dp);
+  PM_CUDA(cudaGetLastError());
+  PM_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev[0], ev[1]);
+  h->timers[0] = ms;
+  h->timers[1] = t_asm;
+  h->timers[2] = t_res;
+  h->timers[3] = t_sol;
+  if (info) *info = loc;
+  return PM_OK;
+}
+
+int pm_get_timers(pm_handle hh, double* t, int n) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !t) return PM_E_ARG;
+  for (int i = 0; i < n && i < 8; ++i) t[i] = h->timers[i];
+  return PM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// pm_internal.h -- handle, device data layout and kernel interfaces of the
+// GB300 Biot hot path.  Shared by the host set-up (pm_setup.cpp), the
+// element kernels (pm_elements.cu) and the C ABI (pm_capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/poromec_gb300.h"
+#include "pm_krylov.h"
+
+namespace pm {
+
+constexpr int kMaxNen = 20;
+constexpr int kNdf = 4;
+
+// Per-material constants of the elastic Biot elements (elmt17_pm,
+// Elmlib03.f:1950-2000; elmt15_pm :190-240), from e(1..7) and |g|.
+struct MatConst {
+  double a, b, c;        // a = E(1-nu)/((1+nu)(1-2nu)), b = nu/(1-nu), c = (1-2nu)/(2(1-nu))
+  double coef_biot;      // alpha
+  double imod_biot;      // 1/M
+  double perm;           // K_h / (rho_f 1e-6 |g|)
+  double pm_d, fluid_d;  // densities * 1e-6
+};
+
+// Node-panel storage of the assembled symmetric matrix (both triangles).
+// The free dofs of a node carry consecutive equation numbers (numeqpmec2),
+// and all rows of a node have the same columns: the free dofs of every node
+// sharing an element with it.  Node I owns a dense d_I x W_I panel stored
+// row-major; its W_I columns are listed once.  The reference CSRD row r of
+// node I (local dof q) is the first low_I + q entries of panel row q.
+struct Panels {
+  int nact = 0;           // nodes with at least one free dof
+  int64_t nnz = 0;        // sum d_I W_I
+  int64_t ncols = 0;      // sum W_I
+  int32_t* eq0 = nullptr;
+  int32_t* d = nullptr;
+  int32_t* W = nullptr;
+  int32_t* low = nullptr;
+  int64_t* val_off = nullptr;
+  int64_t* col_off = nullptr;
+  int32_t* cols = nullptr;
+  double* val = nullptr;   // FP64 values
+  float* val32 = nullptr;  // FP32 values (PM_FP32_REFINE)
+  // indexed by node id - 1
+  int64_t* node_val_off = nullptr;
+  int32_t* node_W = nullptr;
+  PanelView view() const {
+    return PanelView{nact, eq0, d, W, low, val_off, col_off, cols};
+  }
+};
+
+struct ElemLaunch {
+  const int32_t* ix;     // (nen+1, numel)
+  const int32_t* eq;     // (ndf, nnode), 1-based equation numbers
+  const double* x;       // (3, nnode)
+  const MatConst* mat;   // numat
+  const int32_t* slot;   // (nen, nen) per element of the launched colour
+  const int32_t* elems;  // 1-based element ids of the colour
+  int nelem;
+  int nen;
+  const int64_t* node_val_off;
+  const int32_t* node_W;
+  double dt, t;
+  double g0, g1, g2, gmod;
+  int* err;
+};
+
+cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val64,
+                              float* val32, cudaStream_t s);
+cudaError_t launch_residual(const ElemLaunch& L, bool hexa, const double* u,
+                            double* b, cudaStream_t s);
+cudaError_t launch_rhs4(const ElemLaunch& L, bool hexa, const double* u,
+                        const double* dp, const int32_t* eload,
+                        const int32_t* eloadp, const int32_t* load,
+                        const double* fload, int maxt, double* b,
+                        cudaStream_t s);
+cudaError_t launch_stress5(const ElemLaunch& L, bool hexa, const double* tx0,
+                           double* b, cudaStream_t s);
+// Nodal kernels of the step driver (pm_capi.cu).
+struct Handle;
+
+struct Dev {
+  int32_t* ix = nullptr;
+  int32_t* eq = nullptr;
+  double* x = nullptr;
+  MatConst* mat = nullptr;
+  int32_t* slot = nullptr;         // (nen*nen) per element, elements in colour order
+  int32_t* color_elems = nullptr;  // 1-based element ids, colour by colour
+  int32_t* eload = nullptr;
+  int32_t* eloadp = nullptr;
+  int32_t* nload = nullptr;
+  int32_t* load = nullptr;
+  double* fload = nullptr;
+  int32_t* dofkind = nullptr;      // per equation: 0 displacement, 1 pressure
+  int32_t* fnno = nullptr;
+  double *u = nullptr, *u0 = nullptr, *dp = nullptr, *f = nullptr;
+  double *b0 = nullptr, *b = nullptr, *bst0 = nullptr;
+  double *ad = nullptr, *m = nullptr;
+  double *bx = nullptr, *by = nullptr;   // staging vectors for host calls
+  double *rr = nullptr, *dx = nullptr;   // refinement residual / correction
+  double* xs = nullptr;                  // solution of the step's solve
+  KrylovVecs kv{};
+  KrylovScalars* ks = nullptr;
+  double* partial = nullptr;
+  unsigned* counter = nullptr;
+  double* norms = nullptr;
+  int* err = nullptr;
+};
+
+struct Handle {
+  int nnode = 0, nnodev = 0, numel = 0, nen = 0, nenv = 0, ndf = 4, numat = 0;
+  bool hexa = true;
+  int neq = 0;
+  int64_t nad = 0;
+  int numcolors = 0;
+  int precision = PM_FP64;
+  double inner_tol = 1.0e-5;   // inner Krylov tolerance of the FP32 refinement
+  std::vector<int32_t> color_ptr;
+  std::vector<int32_t> h_eq;       // (ndf, nnode)
+  std::vector<int32_t> h_fnno;
+  std::vector<MatConst> h_mat;
+  std::vector<double> h_e;
+  std::vector<int32_t> h_ie;
+  // host copies of the panel structure (pm_get_csrd)
+  std::vector<int32_t> h_eq0, h_d, h_W, h_low, h_cols;
+  std::vector<int64_t> h_val_off, h_col_off;
+  int nloads = 0, maxt = 1;
+  double gravity[3] = {0.0, 0.0, -9.81};
+  double gravity_mod = 9.81;
+  double dt = 1.0, t = 0.0;
+  int istep = 0;
+  bool fstress0 = false;
+  bool assembled = false;      // FP64 panel values valid
+  bool assembled32 = false;    // FP32 panel values valid
+  double assembled_dt = -1.0;
+  double resu0 = 0.0, resp0 = 0.0, res0 = 0.0;
+  Panels P;
+  Dev D;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr;
+  const void* pcg_graph_val = nullptr;   // values pointer baked into the graph
+  const void* minres_graph_val = nullptr;
+  const double* pcg_graph_m = nullptr;
+  double timers[8] = {0};
+  std::string err;
+};
+
+// pm_setup.cpp
+int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
+                    const int32_t* fnno, const double* x, const int32_t* num);
+
+}  // namespace pm

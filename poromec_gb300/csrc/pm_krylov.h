@@ -1,0 +1,75 @@
+// pm_krylov.h -- interfaces of the SpMV and Krylov kernels (pm_sparse.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pm {
+
+// Grid of the SpMV and reduction kernels: 8 CTAs of 256 threads per SM on
+// the 152 SMs of a GB300, so the last-block reductions sum at most 1216
+// partials.
+constexpr int kRedBlocks = 1216;
+
+// Read-only view of the node panels passed by value to kernels.
+struct PanelView {
+  int nact;
+  const int32_t* eq0;      // first equation (0-based) per active node
+  const int32_t* d;        // free dofs per active node
+  const int32_t* W;        // panel width
+  const int32_t* low;      // columns left of the node's own dofs
+  const int64_t* val_off;  // value offset
+  const int64_t* col_off;  // column list offset
+  const int32_t* cols;     // 0-based column equations
+};
+
+// Scalars of one Krylov solve, kept in device memory so that a captured
+// graph of iterations runs without host round trips.
+struct KrylovScalars {
+  double d, bmb, conv, alpha, beta, pq, xkx;
+  double beta_old, normr, neta, c, c_old, s, s_old, ro1, t1, t2, t3, t4;
+  int done;       // set by the first kernel of the iteration after conv_flag
+  int conv_flag;  // 1 converged, 2 iteration limit, 3 breakdown (non-finite)
+  int iter;       // iterations completed (all restarts)
+  int jcycle;     // iterations of the current MINRES cycle
+  int maxit;
+};
+
+struct KrylovVecs {
+  double *x, *r, *z, *p, *q;        // PCG
+  double *v, *v0, *w0, *w00, *z0;   // MINRES (also uses x, z, p, q)
+};
+
+int vec_grid(int n);
+cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
+                 const double* x, double* y, int mode, KrylovScalars* ks,
+                 double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t pcg_init(int n, const double* b, const double* m, KrylovVecs& V,
+                     KrylovScalars* ks, double tol, int maxit, double* partial,
+                     unsigned* counter, cudaStream_t s);
+cudaError_t pcg_iteration(const PanelView& P, const double* val64, const float* val32,
+                          int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
+                          double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t minres_conv(int n, const double* b, const double* m, KrylovScalars* ks,
+                        double tol, double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t minres_start(const PanelView& P, const double* val64, const float* val32,
+                         int n, const double* b, const double* m, KrylovVecs& V,
+                         KrylovScalars* ks, int maxit, bool zero_x, double* partial,
+                         unsigned* counter, cudaStream_t s);
+cudaError_t minres_iteration(const PanelView& P, const double* val64, const float* val32,
+                             int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
+                             double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t csrd_spmv(int neq, const int64_t* ia, const int32_t* ja, const double* ad,
+                      const double* al, const double* x, double* y, cudaStream_t s);
+cudaError_t precond(int n, const double* ad, double* m, int absval, int* zero_diag,
+                    cudaStream_t s);
+cudaError_t panel_diag(const PanelView& P, const double* val64, const float* val32,
+                       double* ad, cudaStream_t s);
+cudaError_t resnorms(int n, const double* b, const int32_t* kind, double* out,
+                     double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t wnorm2(int n, const double* r, const double* m, double* out, double* partial,
+                   unsigned* counter, cudaStream_t s);
+cudaError_t axpy_into(int n, double* y, const double* x, double a, cudaStream_t s);
+cudaError_t vsub(int n, double* y, const double* a, const double* b, cudaStream_t s);
+cudaError_t to_f32(int64_t n, const double* a, float* b, cudaStream_t s);
+
+}  // namespace pm

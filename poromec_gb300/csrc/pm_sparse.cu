@@ -1,0 +1,606 @@
+// pm_sparse.cu -- SpMV and Krylov kernels of the Biot hot path on sm_103a.
+//
+// SpMV over node panels (see Panels in pm_internal.h): one warp per node,
+// the lanes stride along the panel width, so every value row of the panel
+// is read as one coalesced stream and each gathered x value (L2 resident)
+// serves all d rows of the node.  The reduction of the d <= 4 row sums is a
+// warp shuffle tree.  The PCG / MINRES dot products that follow an SpMV are
+// fused into it; every reduction ends with a last-block pass that sums the
+// per-block partials in block order, so results do not depend on scheduling.
+//
+// The Krylov recurrences are those of pcg (Iters.f:299-595) and pminres
+// (Iters.f:3987-4305, sym_ortho :6595).  Each kernel first reads the
+// solver's done flag so a CUDA graph of many iterations can run past
+// convergence without changing the result.
+#include <cuda_runtime.h>
+
+#include "pm_krylov.h"
+
+namespace pm {
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of v (blockDim multiple of 32, <= 1024); result valid in thread 0.
+__device__ double block_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+    v = warp_sum(v);
+  }
+  return v;
+}
+
+// Deterministic grid reduction of up to NV values: each block writes its
+// partial sums; the last block to arrive sums all partials in block order.
+// Returns true in the last block; tot[] valid in its thread 0.
+template <int NV>
+__device__ bool grid_reduce(const double (&v)[NV], double* partial, unsigned* counter,
+                            double (&tot)[NV]) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  double bs[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) bs[k] = block_sum(v[k], sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partial[(size_t)k * gridDim.x + blockIdx.x] = bs[k];
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      s += __ldcg(&partial[(size_t)k * gridDim.x + i]);
+    tot[k] = block_sum(s, sh);
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+// Early exit shared by the per-iteration kernels.  conv_flag is set by the
+// reduction that detects convergence; the first kernel of the next
+// iteration turns it into done, which every later kernel reads.
+__device__ __forceinline__ bool krylov_skip(KrylovScalars* ks, bool first) {
+  if (ks->done) return true;
+  if (first && ks->conv_flag) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ks->done = 1;
+    return true;
+  }
+  return false;
+}
+
+// ---- SpMV over panels ------------------------------------------------------
+// MODE 0: y = A x.   MODE 1: PCG, also alpha = d / (y . x).
+// MODE 2: MINRES, also alpha = |x . y| / beta^2.   MODE 3: y = A x and
+// ks->xkx = x . y (energy norm of the solver log).
+template <typename TV, int MODE>
+__global__ void __launch_bounds__(256)
+    k_spmv(PanelView P, const TV* __restrict__ val, const double* __restrict__ x,
+           double* __restrict__ y, KrylovScalars* ks, double* partial,
+           unsigned* counter) {
+  if (MODE == 1 || MODE == 2)
+    if (krylov_skip(ks, true)) return;
+  const int lane = threadIdx.x & 31;
+  const int wid = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+  double dsum = 0.0;
+  for (int node = wid; node < P.nact; node += nw) {
+    const int e0 = P.eq0[node], d = P.d[node], W = P.W[node];
+    const TV* v = val + P.val_off[node];
+    const int32_t* cols = P.cols + P.col_off[node];
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (d == 4) {
+      for (int c = lane; c < W; c += 32) {
+        const double xv = x[cols[c]];
+        a0 += double(v[c]) * xv;
+        a1 += double(v[W + c]) * xv;
+        a2 += double(v[2 * W + c]) * xv;
+        a3 += double(v[3 * W + c]) * xv;
+      }
+    } else if (d == 3) {
+      for (int c = lane; c < W; c += 32) {
+        const double xv = x[cols[c]];
+        a0 += double(v[c]) * xv;
+        a1 += double(v[W + c]) * xv;
+        a2 += double(v[2 * W + c]) * xv;
+      }
+    } else {
+      for (int c = lane; c < W; c += 32) {
+        const double xv = x[cols[c]];
+        a0 += double(v[c]) * xv;
+        if (d > 1) a1 += double(v[W + c]) * xv;
+        if (d > 2) a2 += double(v[2 * W + c]) * xv;
+      }
+    }
+    a0 = warp_sum(a0);
+    if (d > 1) a1 = warp_sum(a1);
+    if (d > 2) a2 = warp_sum(a2);
+    if (d > 3) a3 = warp_sum(a3);
+    if (lane < d) {
+      const double yv = lane == 0 ? a0 : lane == 1 ? a1 : lane == 2 ? a2 : a3;
+      y[e0 + lane] = yv;
+      if (MODE != 0) dsum += yv * x[e0 + lane];
+    }
+  }
+  if (MODE != 0) {
+    double in[1] = {dsum}, tot[1];
+    if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+      if (MODE == 1) {
+        ks->pq = tot[0];
+        ks->alpha = ks->d / tot[0];
+      } else if (MODE == 2) {
+        ks->alpha = fabs(tot[0]) * (1.0 / (ks->beta * ks->beta));
+      } else {
+        ks->xkx = tot[0];
+      }
+    }
+  }
+}
+
+// ---- PCG -------------------------------------------------------------------
+// r = b, z = m r, p = z, d = (r, z); conv = tol sqrt|(b, m b)|  (x0 = 0, so
+// b - A x0 = b exactly)
+__global__ void __launch_bounds__(256)
+    k_pcg_init(int n, const double* __restrict__ b, const double* __restrict__ m,
+               double* __restrict__ r, double* __restrict__ z, double* __restrict__ p,
+               double* __restrict__ x, KrylovScalars* ks, double tol, int maxit,
+               double* partial, unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double bi = b[i], zi = bi * m[i];
+    x[i] = 0.0;
+    r[i] = bi;
+    z[i] = zi;
+    p[i] = zi;
+    acc += bi * zi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    ks->d = tot[0];
+    ks->bmb = tot[0];
+    ks->conv = tol * sqrt(fabs(tot[0]));
+    ks->done = 0;
+    ks->conv_flag = 0;
+    ks->iter = 0;
+    ks->maxit = maxit;
+  }
+}
+
+// x += alpha p, r -= alpha q, z = m r, di = (r, z), beta = di / d, d = di;
+// converged when sqrt|d| < conv (Iters.f:446-497).
+__global__ void __launch_bounds__(256)
+    k_pcg_update(int n, double* __restrict__ x, const double* __restrict__ p,
+                 double* __restrict__ r, const double* __restrict__ q,
+                 const double* __restrict__ m, double* __restrict__ z,
+                 KrylovScalars* ks, double* partial, unsigned* counter) {
+  if (krylov_skip(ks, false)) return;
+  const double alpha = ks->alpha;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = x[i] + alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const double zi = ri * m[i];
+    z[i] = zi;
+    acc += ri * zi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    const double di = tot[0];
+    ks->beta = di / ks->d;
+    ks->d = di;
+    ks->iter += 1;
+    if (sqrt(fabs(di)) < ks->conv) ks->conv_flag = 1;
+    else if (!isfinite(di)) ks->conv_flag = 3;  // breakdown: stop instead of iterating on NaN
+    else if (ks->iter >= ks->maxit) ks->conv_flag = 2;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_pcg_dir(int n, const double* __restrict__ z, double* __restrict__ p,
+              KrylovScalars* ks) {
+  if (krylov_skip(ks, false)) return;
+  const double beta = ks->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+// ---- MINRES ----------------------------------------------------------------
+__device__ double sign1(double a) { return a > 0.0 ? 1.0 : (a < 0.0 ? -1.0 : 0.0); }
+
+// sym_ortho (Iters.f:6595-6640); c, s, r keep their values in the branch the
+// reference leaves uncovered (b != 0, a > 0, |b| == a).
+__device__ void sym_ortho(double a, double b, double& c, double& s, double& r) {
+  const double ma = fabs(a), mb = fabs(b), sa = sign1(a), sb = sign1(b);
+  if (b == 0.0) {
+    s = 0.0;
+    r = ma;
+    c = (a == 0.0) ? 1.0 : sa;
+  } else if (a == 0.0) {
+    c = 0.0;
+    s = sb;
+    r = mb;
+  } else if (mb > a) {
+    const double t = a / b;
+    s = sb / sqrt(1.0 + t * t);
+    c = s * t;
+    r = b / s;
+  } else if (ma > mb) {
+    const double t = b / a;
+    c = sa / sqrt(1.0 + t * t);
+    s = c * t;
+    r = a / c;
+  }
+}
+
+// conv = tol * || M^(1/2) b || with M = |m| (Iters.f:4082-4088)
+__global__ void __launch_bounds__(256)
+    k_minres_conv(int n, const double* __restrict__ b, const double* __restrict__ m,
+                  KrylovScalars* ks, double tol, double* partial, unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double zi = b[i] * sqrt(fabs(m[i]));
+    acc += zi * zi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0)
+    ks->conv = tol * sqrt(fabs(tot[0]));
+}
+
+// (Re)start: v = b - A x (q = A x), v0 = w0 = w00 = 0, z0 = m v,
+// beta = sqrt|(v, z0)| (Iters.f:4100-4131)
+__global__ void __launch_bounds__(256)
+    k_minres_start(int n, const double* __restrict__ b, const double* __restrict__ q,
+                   const double* __restrict__ m, double* __restrict__ v,
+                   double* __restrict__ v0, double* __restrict__ w0,
+                   double* __restrict__ w00, double* __restrict__ z0, KrylovScalars* ks,
+                   int maxit, double* partial, unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double vi = b[i] - q[i];
+    v[i] = vi;
+    v0[i] = 0.0;
+    w0[i] = 0.0;
+    w00[i] = 0.0;
+    const double zi = vi * m[i];
+    z0[i] = zi;
+    acc += vi * zi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    const double beta = sqrt(fabs(tot[0]));
+    ks->beta = beta;
+    ks->normr = beta;
+    ks->neta = beta;
+    ks->beta_old = beta;
+    ks->c_old = 1.0;
+    ks->c = 1.0;
+    ks->s_old = 0.0;
+    ks->s = 0.0;
+    ks->done = 0;
+    ks->conv_flag = 0;
+    ks->jcycle = 0;
+    ks->maxit = maxit;
+  }
+}
+
+// p = (A z0)/beta - alpha v/beta - beta v0/beta_old, z = m p,
+// beta_new = sqrt|(z, p)|, then the QR update of the tridiagonal
+// (Iters.f:4143-4200).
+__global__ void __launch_bounds__(256)
+    k_minres_lanczos(int n, double* __restrict__ p, const double* __restrict__ v,
+                     const double* __restrict__ v0, const double* __restrict__ m,
+                     double* __restrict__ z, KrylovScalars* ks, double* partial,
+                     unsigned* counter) {
+  if (krylov_skip(ks, false)) return;
+  const double beta = ks->beta;
+  const double t1 = 1.0 / beta, t2 = -ks->alpha / beta, t3 = -beta / ks->beta_old;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double pi = t1 * p[i] + t2 * v[i] + t3 * v0[i];
+    p[i] = pi;
+    const double zi = pi * m[i];
+    z[i] = zi;
+    acc += zi * pi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    const double alpha = ks->alpha;
+    const double beta_old = beta;
+    const double beta_new = sqrt(fabs(tot[0]));
+    double c = ks->c, s = ks->s;
+    const double c_old = ks->c_old, s_old = ks->s_old;
+    const double delta = c * alpha - c_old * s * beta_old;
+    const double ro2 = s * alpha + c_old * c * beta_old;
+    const double ro3 = s_old * beta_old;
+    ks->c_old = c;
+    ks->s_old = s;
+    double ro1 = ks->ro1;
+    sym_ortho(delta, beta_new, c, s, ro1);
+    ks->c = c;
+    ks->s = s;
+    ks->ro1 = ro1;
+    ks->beta_old = beta_old;
+    ks->beta = beta_new;
+    ks->t1 = 1.0 / (beta_old * ro1);
+    ks->t2 = -ro2 / ro1;
+    ks->t3 = -ro3 / ro1;
+    ks->t4 = c * ks->neta;
+    ks->normr = fabs(s) * ks->normr;
+    ks->iter += 1;
+    ks->jcycle += 1;
+    if (ks->normr < ks->conv) {
+      ks->conv_flag = 1;
+    } else if (!isfinite(ks->normr)) {
+      ks->conv_flag = 3;
+    } else {
+      ks->neta = -s * ks->neta;
+      if (ks->jcycle >= ks->maxit) ks->conv_flag = 2;
+    }
+  }
+}
+
+// w = t1 z0 + t2 w0 + t3 w00, x += t4 w, then the shifts v0 = v, v = p,
+// z0 = z, w00 = w0, w0 = w (Iters.f:4202-4222).
+__global__ void __launch_bounds__(256)
+    k_minres_update(int n, double* __restrict__ x, double* __restrict__ z0,
+                    double* __restrict__ w0, double* __restrict__ w00,
+                    double* __restrict__ v0, double* __restrict__ v,
+                    const double* __restrict__ p, const double* __restrict__ z,
+                    KrylovScalars* ks) {
+  if (krylov_skip(ks, false)) return;
+  const double t1 = ks->t1, t2 = ks->t2, t3 = ks->t3, t4 = ks->t4;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double wi = t1 * z0[i] + t2 * w0[i] + t3 * w00[i];
+    x[i] = x[i] + t4 * wi;
+    v0[i] = v[i];
+    v[i] = p[i];
+    z0[i] = z[i];
+    w00[i] = w0[i];
+    w0[i] = wi;
+  }
+}
+
+// ---- reference CSRD layout --------------------------------------------------
+// y = (D + L + L^T) x for the lower CSR of Matvec.f:1504-1598 (1-based ia,
+// ja); the transposed part is scattered with FP64 atomics.  y must be zero.
+__global__ void __launch_bounds__(256)
+    k_csrd_spmv(int neq, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja,
+                const double* __restrict__ ad, const double* __restrict__ al,
+                const double* __restrict__ x, double* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < neq; i += nw) {
+    const double xi = x[i];
+    double t = 0.0;
+    for (int64_t k = ia[i] - 1 + lane; k < ia[i + 1] - 1; k += 32) {
+      const int j = ja[k] - 1;
+      const double s = al[k];
+      t += s * x[j];
+      atomicAdd(&y[j], s * xi);
+    }
+    t = warp_sum(t);
+    if (lane == 0) atomicAdd(&y[i], t + ad[i] * xi);
+  }
+}
+
+// ---- small vector kernels --------------------------------------------------
+__global__ void k_precond(int n, const double* __restrict__ ad, double* __restrict__ m,
+                          int absval, int* zero_diag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double a = ad[i];
+    if (a == 0.0) atomicOr(zero_diag, 1);
+    const double v = 1.0 / a;
+    m[i] = absval ? fabs(v) : v;
+  }
+}
+
+// Panel diagonal -> ad (the diagonal of the node's own block).
+template <typename TV>
+__global__ void k_diag(PanelView P, const TV* __restrict__ val, double* __restrict__ ad) {
+  for (int node = blockIdx.x * blockDim.x + threadIdx.x; node < P.nact;
+       node += gridDim.x * blockDim.x) {
+    const int e0 = P.eq0[node], d = P.d[node], W = P.W[node], low = P.low[node];
+    const TV* v = val + P.val_off[node];
+    for (int r = 0; r < d; ++r) ad[e0 + r] = double(v[(int64_t)r * W + low + r]);
+  }
+}
+
+// Residual norms of cal_residuo_pm: sum of squares of b over displacement
+// and pressure equations (stop_crit 2) and over all (stop_crit 1).
+__global__ void __launch_bounds__(256)
+    k_resnorms(int n, const double* __restrict__ b, const int32_t* __restrict__ kind,
+               double* out, double* partial, unsigned* counter) {
+  double au = 0.0, ap = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double bi = b[i];
+    if (kind[i]) ap += bi * bi;
+    else au += bi * bi;
+  }
+  double in[2] = {au, ap}, tot[2];
+  if (grid_reduce<2>(in, partial, counter, tot) && threadIdx.x == 0) {
+    out[0] = tot[0];
+    out[1] = tot[1];
+  }
+}
+
+// sum |m_i| r_i^2 (the refinement loop's residual norm)
+__global__ void __launch_bounds__(256)
+    k_wnorm2(int n, const double* __restrict__ r, const double* __restrict__ m, double* out,
+             double* partial, unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    acc += fabs(m[i]) * r[i] * r[i];
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) out[0] = tot[0];
+}
+
+__global__ void k_axpy_into(int n, double* __restrict__ y, const double* __restrict__ x,
+                            double a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = y[i] + a * x[i];
+}
+
+__global__ void k_sub(int n, double* __restrict__ y, const double* __restrict__ a,
+                      const double* __restrict__ b) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = a[i] - b[i];
+}
+
+// FP64 panel values -> FP32 copy (PM_FP32_REFINE with FP64 assembly).
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = float(a[i]);
+}
+
+}  // namespace
+
+int vec_grid(int n) {
+  int g = (n + 255) / 256;
+  return g < 1 ? 1 : (g > kRedBlocks ? kRedBlocks : g);
+}
+
+cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
+                 const double* x, double* y, int mode, KrylovScalars* ks,
+                 double* partial, unsigned* counter, cudaStream_t s) {
+  const int grid = kRedBlocks;
+  if (val32) {
+    switch (mode) {
+      case 0: k_spmv<float, 0><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
+      case 1: k_spmv<float, 1><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
+      case 2: k_spmv<float, 2><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
+      default: k_spmv<float, 3><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
+    }
+  } else {
+    switch (mode) {
+      case 0: k_spmv<double, 0><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+      case 1: k_spmv<double, 1><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+      case 2: k_spmv<double, 2><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+      default: k_spmv<double, 3><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t pcg_init(int n, const double* b, const double* m, KrylovVecs& V,
+                     KrylovScalars* ks, double tol, int maxit, double* partial,
+                     unsigned* counter, cudaStream_t s) {
+  k_pcg_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.r, V.z, V.p, V.x, ks, tol, maxit,
+                                          partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t pcg_iteration(const PanelView& P, const double* val64, const float* val32,
+                          int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
+                          double* partial, unsigned* counter, cudaStream_t s) {
+  cudaError_t e = spmv(P, val64, val32, V.p, V.q, 1, ks, partial, counter, s);
+  if (e != cudaSuccess) return e;
+  k_pcg_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, m, V.z, ks, partial,
+                                            counter);
+  k_pcg_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t minres_conv(int n, const double* b, const double* m, KrylovScalars* ks,
+                        double tol, double* partial, unsigned* counter, cudaStream_t s) {
+  k_minres_conv<<<vec_grid(n), 256, 0, s>>>(n, b, m, ks, tol, partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t minres_start(const PanelView& P, const double* val64, const float* val32,
+                         int n, const double* b, const double* m, KrylovVecs& V,
+                         KrylovScalars* ks, int maxit, bool zero_x, double* partial,
+                         unsigned* counter, cudaStream_t s) {
+  if (zero_x) {
+    cudaMemsetAsync(V.x, 0, sizeof(double) * n, s);
+    cudaMemsetAsync(V.q, 0, sizeof(double) * n, s);
+  } else {
+    cudaError_t e = spmv(P, val64, val32, V.x, V.q, 0, ks, partial, counter, s);
+    if (e != cudaSuccess) return e;
+  }
+  k_minres_start<<<vec_grid(n), 256, 0, s>>>(n, b, V.q, m, V.v, V.v0, V.w0, V.w00, V.z0,
+                                              ks, maxit, partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t minres_iteration(const PanelView& P, const double* val64, const float* val32,
+                             int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
+                             double* partial, unsigned* counter, cudaStream_t s) {
+  cudaError_t e = spmv(P, val64, val32, V.z0, V.p, 2, ks, partial, counter, s);
+  if (e != cudaSuccess) return e;
+  k_minres_lanczos<<<vec_grid(n), 256, 0, s>>>(n, V.p, V.v, V.v0, m, V.z, ks, partial,
+                                                counter);
+  k_minres_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.z0, V.w0, V.w00, V.v0, V.v, V.p,
+                                               V.z, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t csrd_spmv(int neq, const int64_t* ia, const int32_t* ja, const double* ad,
+                      const double* al, const double* x, double* y, cudaStream_t s) {
+  cudaMemsetAsync(y, 0, sizeof(double) * neq, s);
+  int grid = (neq + 7) / 8;
+  if (grid > 8 * kRedBlocks) grid = 8 * kRedBlocks;
+  if (grid < 1) grid = 1;
+  k_csrd_spmv<<<grid, 256, 0, s>>>(neq, ia, ja, ad, al, x, y);
+  return cudaGetLastError();
+}
+
+cudaError_t precond(int n, const double* ad, double* m, int absval, int* zero_diag,
+                    cudaStream_t s) {
+  k_precond<<<vec_grid(n), 256, 0, s>>>(n, ad, m, absval, zero_diag);
+  return cudaGetLastError();
+}
+
+cudaError_t panel_diag(const PanelView& P, const double* val64, const float* val32,
+                       double* ad, cudaStream_t s) {
+  const int g = vec_grid(P.nact);
+  if (val32) k_diag<float><<<g, 256, 0, s>>>(P, val32, ad);
+  else k_diag<double><<<g, 256, 0, s>>>(P, val64, ad);
+  return cudaGetLastError();
+}
+
+cudaError_t resnorms(int n, const double* b, const int32_t* kind, double* out,
+                     double* partial, unsigned* counter, cudaStream_t s) {
+  k_resnorms<<<vec_grid(n), 256, 0, s>>>(n, b, kind, out, partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t wnorm2(int n, const double* r, const double* m, double* out, double* partial,
+                   unsigned* counter, cudaStream_t s) {
+  k_wnorm2<<<vec_grid(n), 256, 0, s>>>(n, r, m, out, partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t axpy_into(int n, double* y, const double* x, double a, cudaStream_t s) {
+  k_axpy_into<<<vec_grid(n), 256, 0, s>>>(n, y, x, a);
+  return cudaGetLastError();
+}
+
+cudaError_t vsub(int n, double* y, const double* a, const double* b, cudaStream_t s) {
+  k_sub<<<vec_grid(n), 256, 0, s>>>(n, y, a, b);
+  return cudaGetLastError();
+}
+
+cudaError_t to_f32(int64_t n, const double* a, float* b, cudaStream_t s) {
+  int64_t g = (n + 255) / 256;
+  if (g > 8 * kRedBlocks) g = 8 * kRedBlocks;
+  k_to_f32<<<(int)g, 256, 0, s>>>(n, a, b);
+  return cudaGetLastError();
+}
+
+}  // namespace pm

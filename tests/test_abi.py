@@ -1,0 +1,87 @@
+"""CPU-side checks of the C ABI and the host code (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from poromec_gb300 import build as gbuild
+from poromec_gb300 import meshgen
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "poromec_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(pm_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    lib_path = gbuild.build()
+    lib = ctypes.CDLL(lib_path)
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+
+
+def test_status_strings_without_gpu():
+    lib = ctypes.CDLL(gbuild.build())
+    lib.pm_status_string.restype = ctypes.c_char_p
+    assert lib.pm_status_string(0) == b"ok"
+    assert b"converge" in lib.pm_status_string(4)
+
+
+def test_create_rejects_bad_arguments_without_touching_the_gpu():
+    lib = ctypes.CDLL(gbuild.build())
+    h = ctypes.c_void_p()
+    # nen/nenv mismatch is rejected before any CUDA call
+    st = lib.pm_mesh_create(10, 8, 1, 20, 4, 3, 4, None, None, None, None, 1, None, None,
+                            None, ctypes.byref(h))
+    assert st == 1
+
+
+def test_hexa_mesh_generator():
+    m = meshgen.hexa20_box(2, 3, 4, 1.0, 2.0, 3.0)
+    assert m["numel"] == 24
+    nv = 3 * 4 * 5
+    assert m["nnodev"] == nv
+    # vertices + one mid-edge node per edge
+    edges = 2 * 4 * 5 + 3 * 3 * 5 + 3 * 4 * 4
+    assert m["nnode"] == nv + edges
+    ix = m["ix"]
+    x = m["x"]
+    # every element: positive Jacobian of the reference's vertex order
+    v = x[ix[:, :8] - 1]
+    assert np.all(v[:, 0, 0] > v[:, 1, 0]) and np.all(v[:, 0, 2] > v[:, 4, 2])
+    mid = x[ix[:, 8] - 1]
+    assert np.allclose(mid, 0.5 * (v[:, 0] + v[:, 1]))
+
+
+def test_tetra_mesh_generator_orientation():
+    m = meshgen.tetra10_kuhn_box(3, 3, 3, jitter=0.1, seed=1)
+    assert m["numel"] == 6 * 27
+    assert m["nnode"] == 7 ** 3
+    x = m["x"]
+    P = x[m["ix"][:, :4] - 1]
+    det = np.einsum("ij,ij->i", P[:, 0] - P[:, 3], np.cross(P[:, 1] - P[:, 3], P[:, 2] - P[:, 3]))
+    assert np.all(det > 0)
+
+
+def test_random_field_moments():
+    f = meshgen.gaussian_random_field((24, 24, 24), 0.1, (1 / 24,) * 3, seed=3)
+    assert abs(f.mean()) < 1e-12 and abs(f.std() - 1) < 1e-12
+    g = meshgen.gaussian_random_field((24, 24, 24), 0.1, (1 / 24,) * 3, seed=3)
+    assert np.array_equal(f, g)
+
+
+@pytest.mark.parametrize("nen", [20, 10])
+def test_oracle_flop_count(nen):
+    import oracle
+    f = oracle.element_flops(nen)
+    if nen == 20:
+        assert 1.8e6 < f < 1.95e6
+    else:
+        assert 2e4 < f < 5e4

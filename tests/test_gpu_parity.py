@@ -1,0 +1,229 @@
+"""GPU parity: the C-ABI library against the CPU oracle and the reference's
+golden runs.
+
+Tolerances: index work (equation numbers, CSRD ia/ja) is compared bit for
+bit; FP64 assembly entries within 1e-12 of the matrix's largest entry in the
+row block; solutions within 1e-10 relative (the plain FP64 bar); golden node
+histories within 1e-10 absolute (the reference prints 10 decimals).
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+import poromec_gb300 as pg  # noqa: E402
+from poromec_gb300 import meshgen  # noqa: E402
+
+GOLDEN_CASES = ["exemplo1_mesh0_t2", "exemplo1_mesh0_t2_tetra"]
+
+
+def _pair(pb):
+    m = pg.from_problem(pb)
+    o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]), int(pb["nen"]),
+                      int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"])
+    has = "load" in pb and len(pb["load"]) > 0
+    o.set_loads(eload=pb.get("eload"), nload=pb.get("nload"),
+                load=pb["load"] if has else None, fload=pb["fload"] if has else None)
+    o.set_env(pb["gravity"], float(pb["dt"]))
+    o.set_state(u=pb["u0"], u0=pb["u0"])
+    return m, o
+
+
+def _problems(golden):
+    out = [golden(n) for n in GOLDEN_CASES]
+    out.append(meshgen.column_problem())
+    out.append(meshgen.tetra_problem(n=3))
+    c = meshgen.cube_problem(n=4)
+    out.append(c)
+    return out
+
+
+@pytest.fixture(scope="module")
+def problems(golden):
+    return _problems(golden)
+
+
+def test_numbering_and_pattern_bit_exact(problems):
+    for pb in problems:
+        m, o = _pair(pb)
+        assert m.neq == o.neq and m.nad == o.nad
+        assert np.array_equal(m.get_id(), o.get_id())
+        ia, ja, _, _ = m.get_csrd(values=False)
+        ia_o, ja_o, _, _ = o.get_csrd()
+        assert np.array_equal(ia, ia_o)
+        assert np.array_equal(ja, ja_o)
+
+
+def test_assembly_matches_oracle(problems):
+    rng = np.random.default_rng(0)
+    for pb in problems:
+        m, o = _pair(pb)
+        du = rng.standard_normal((m.nnode, 4)) * 1e-3
+        b = rng.standard_normal(m.neq)
+        bg, bo = b.copy(), b.copy()
+        m.pform(2, True, True, du, bg)
+        o.pform(2, True, True, du, bo)
+        _, _, ad, al = m.get_csrd()
+        _, _, ado, alo = o.get_csrd()
+        scale = max(np.abs(ado).max(), np.abs(alo).max())
+        assert np.abs(ad - ado).max() <= 1e-12 * scale
+        assert np.abs(al - alo).max() <= 1e-12 * scale
+        assert np.abs(bg - bo).max() <= 1e-11 * max(1.0, np.abs(bo).max())
+
+
+def test_rhs_isw4_matches_oracle(problems):
+    rng = np.random.default_rng(1)
+    for pb in problems:
+        m, o = _pair(pb)
+        u = pb["u0"] + rng.standard_normal((m.nnode, 4)) * 1e-3
+        dp = rng.standard_normal(m.nnode) * 1e-3
+        m.set_state(dp=dp)
+        o.set_state(dp=dp)
+        b = np.zeros(m.neq)
+        bg, bo = b.copy(), b.copy()
+        m.pform(4, False, True, u, bg)
+        o.pform(4, False, True, u, bo)
+        assert np.abs(bg - bo).max() <= 1e-11 * max(1e-12, np.abs(bo).max())
+
+
+def test_spmv_matches_oracle(problems):
+    rng = np.random.default_rng(2)
+    for pb in problems:
+        m, o = _pair(pb)
+        du = np.zeros((m.nnode, 4))
+        m.pform(2, True, False, du, None)
+        _, _, ad, al = m.get_csrd()
+        o.set_csrd_values(ad, al)  # same values on both sides
+        x = rng.standard_normal(m.neq)
+        y = m.matvec(x)
+        yo = o.matvec(x)
+        assert np.abs(y - yo).max() <= 1e-13 * np.abs(yo).max()
+        yo4 = o.matvec(x, nthreads=4)
+        assert np.abs(yo4 - yo).max() <= 1e-13 * np.abs(yo).max()
+
+
+def test_csrd_reference_layout_on_device(problems):
+    pb = problems[0]
+    m, o = _pair(pb)
+    m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+    ia, ja, ad, al = m.get_csrd()
+    o.set_csrd_values(ad, al)
+    x = np.random.default_rng(3).standard_normal(m.neq)
+    t = {k: torch.from_numpy(v).cuda() for k, v in dict(ia=ia, ja=ja, ad=ad, al=al, x=x).items()}
+    y = torch.empty(m.neq, dtype=torch.float64, device="cuda")
+    pg.matvec_csrd_dev(m.neq, t["ia"].data_ptr(), t["ja"].data_ptr(), t["ad"].data_ptr(),
+                       t["al"].data_ptr(), t["x"].data_ptr(), y.data_ptr(),
+                       torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    yo = o.matvec(x)
+    assert np.abs(y.cpu().numpy() - yo).max() <= 1e-13 * np.abs(yo).max()
+
+
+@pytest.mark.parametrize("solver,precond", [(1, 2), (7, 5)])
+def test_solve_matches_oracle(problems, solver, precond):
+    for pb in problems[:3]:
+        m, o = _pair(pb)
+        m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+        _, _, ad, al = m.get_csrd()
+        o.set_csrd_values(ad, al)
+        b = np.random.default_rng(4).standard_normal(m.neq)
+        x, info = m.solve(b, solver=solver, precond=precond, tol=1e-12, maxit=200000)
+        xo, info_o = o.solve(b, solver=solver, precond=precond, tol=1e-12, maxit=200000)
+        assert np.abs(x - xo).max() <= 1e-9 * np.abs(xo).max()
+        assert abs(info.iters - info_o.iters) <= max(3, 0.1 * info_o.iters)
+
+
+def test_solve_dev_torch_tensors(problems):
+    pb = problems[2]
+    m, o = _pair(pb)
+    m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+    b = np.random.default_rng(5).standard_normal(m.neq)
+    x_ref, _ = m.solve(b, tol=1e-11)
+    bt = torch.from_numpy(b).cuda()
+    xt = torch.empty_like(bt)
+    m.solve_dev(bt.data_ptr(), xt.data_ptr(), tol=1e-11,
+                stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(xt.cpu().numpy(), x_ref)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_histories_on_gpu(golden, name):
+    fx = golden(name)
+    m = pg.from_problem(fx)
+    worst = 0.0
+    for k in range(1, 601):
+        m.step(maxnlit=2, stop_crit=1, solvtol=float(fx["solver_tol"]), maxit=int(fx["maxit"]))
+        u, _, _ = m.get_state()
+        for a, n in enumerate(fx["hist_nodes"]):
+            worst = max(worst, np.abs(u[n - 1] - fx["hist"][a][k][2:6]).max())
+    assert worst < 1e-10, worst
+
+
+def test_column_steps_match_oracle():
+    pb = meshgen.column_problem()
+    m, o = _pair(pb)
+    for k in range(20):
+        gi = m.step(maxnlit=2, stop_crit=2, solvtol=1e-10)
+        oi = o.step(maxnlit=2, stop_crit=2, solvtol=1e-10)
+        u, u0, dp = m.get_state()
+        uo, u0o, dpo = o.get_state()
+        for comp, sl in (("u", slice(0, 3)), ("p", slice(3, 4))):
+            ref = uo[:, sl]
+            err = np.abs(u[:, sl] - ref).max() / np.abs(ref).max()
+            assert err < 1e-10, (k, comp, err)
+        assert gi.nlit == oi.nlit
+
+
+def test_stop_crit2_reference_semantics(golden):
+    """With stop_crit 2 the reference resets the pressure reference norm to
+    max(resp0, gresu) on the second iteration (Residuo.f); on the hydrostatic
+    golden column this makes the check fail, so the step reports
+    non-convergence like the reference's stop_mef."""
+    fx = golden("exemplo1_mesh0_t2")
+    m = pg.from_problem(fx)
+    with pytest.raises(pg.PMError) as e:
+        m.step(maxnlit=2, stop_crit=2, solvtol=float(fx["solver_tol"]))
+    assert e.value.status == 5
+
+
+def test_mixed_precision_refinement():
+    pb = meshgen.cube_problem(n=6)
+    m64 = pg.from_problem(pb)
+    m32 = pg.from_problem(pb)
+    m32.set_precision(pg.capi.PM_FP32_REFINE)
+    for k in range(3):
+        m64.step(maxnlit=2, stop_crit=1, solvtol=1e-10)
+        info = m32.step(maxnlit=2, stop_crit=1, solvtol=1e-10)
+        assert info.refine >= 1
+    u, _, _ = m64.get_state()
+    v, _, _ = m32.get_state()
+    for sl in (slice(0, 3), slice(3, 4)):
+        assert np.abs(u[:, sl] - v[:, sl]).max() <= 1e-8 * np.abs(u[:, sl]).max()
+
+
+def test_errors_are_returned_not_fatal(problems):
+    # maxit exceeded -> status 4, and the handle stays usable
+    pb = problems[2]
+    m, _ = _pair(pb)
+    m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+    b = np.ones(m.neq)
+    with pytest.raises(pg.PMError) as e:
+        m.solve(b, maxit=1, tol=1e-14)
+    assert e.value.status == 4
+    x, _ = m.solve(b, tol=1e-10)
+    assert np.isfinite(x).all()
+    # inverted element -> status 2 (det <= 1e-14), no fault
+    bad = dict(pb)
+    bad["x"] = pb["x"].copy()
+    bad["x"][:, 2] *= -1.0
+    mb = pg.from_problem(bad)
+    with pytest.raises(pg.PMError) as e:
+        mb.pform(2, True, False, np.zeros((mb.nnode, 4)), None)
+    assert e.value.status == 2
