@@ -1,0 +1,360 @@
+"""Benchmark: implicit-Euler Biot steps/s of the heterogeneous hexa20 cube.
+
+Workload (the BASELINE metric's configuration that fits one GPU): structured
+56^3 hexa20 mesh of the unit cube, 731,025 nodes, 2,346,120 free equations
+(2.38 M dofs before boundary conditions), log-permeability Gaussian random
+field (mean ln 1e-14 m^2, sigma 1, correlation length 0.1 m), lognormal E
+(median 1 GPa, sigma_ln 0.3), nu = 0.25, base fixed, drained top, top
+traction ramped to 5 MPa over 10 steps of 100 s; seeded synthetic inputs.
+
+One step = the reference's 'solv' macro (Main.f:876-1123): nodal loads,
+isw 4 element loop, K re-assembled from the elements (isw 2, as the
+reference does every step), residual, diagonal-PCG solve to 1e-8, residual
+check, state update.  `value` is steps/s with the state resident in HBM;
+`e2e` is the same step through the C ABI with the nodal state copied from
+and back to pinned host buffers every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs N independent replicas (one per GPU; a single mesh does not
+shard without the halo exchange of the reference's MPI path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Biot steps/s at 2M dof: FP64 plain vs FP32+refine at 1e-8 rel; SpMV HBM GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=56, help="elements per cube edge")
+    ap.add_argument("--solvtol", type=float, default=1e-8)
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def spmv_bytes(nad, neq):
+    """Algorithmic bytes of one CSRD SpMV (FP64): each stored lower value and
+    its int32 column once, ad, x, y and the int32 row pointer once."""
+    return 12 * nad + 28 * neq
+
+
+def profile_traffic(nnz_panel):
+    """DRAM bytes per SpMV launch from the committed ncu summary (bytes per
+    panel nonzero measured on a smaller cube, scaled to this launch)."""
+    p = os.path.join(ROOT, "profiles", "spmv_panel_fp64_cube.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_panel_nnz:"):
+            try:
+                return float(line.split(":")[1]) * nnz_panel
+            except ValueError:
+                return None
+    return None
+
+
+# --------------------------------------------------------------------------
+# CPU arm: the oracle (a restatement of the reference's Fortran with its
+# OpenMP design: coloured element loop, row-partitioned CSRD SpMV) timed on a
+# bounded sample of the same step, on all host cores.
+# --------------------------------------------------------------------------
+def cpu_step_estimate(pb, iters, elem_sample=600, pcg_sample=4, threads=None):
+    import oracle
+    threads = threads or os.cpu_count()
+    o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]), int(pb["nen"]),
+                      int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"])
+    o.set_loads(eload=pb["eload"], load=pb["load"], fload=pb["fload"])
+    o.set_env(pb["gravity"], float(pb["dt"]))
+    o.set_state(u=pb["u0"], u0=pb["u0"])
+    numel = int(pb["numel"])
+    b = np.zeros(o.neq)
+    du = np.zeros((int(pb["nnode"]), 4))
+    S = min(elem_sample, numel)
+    t0 = time.perf_counter()
+    o.pform_range(4, 0, 1, pb["u0"], b, threads, 1, S + 1)
+    t4 = (time.perf_counter() - t0) * numel / S
+    t0 = time.perf_counter()
+    o.pform_range(2, 1, 1, du, b, threads, 1, S + 1)
+    t2l = (time.perf_counter() - t0) * numel / S
+    t0 = time.perf_counter()
+    o.pform_range(2, 0, 1, du, b, threads, 1, S + 1)
+    t2r = (time.perf_counter() - t0) * numel / S
+    # PCG iterations: the cost per iteration does not depend on the values
+    o.set_csrd_values(np.ones(o.neq), np.full(o.nad, 1e-6))
+    rhs = np.ones(o.neq)
+    t0 = time.perf_counter()
+    try:
+        o.solve(rhs, tol=1e-300, maxit=pcg_sample, nthreads=threads)
+    except oracle.OracleError:
+        pass
+    t_it = (time.perf_counter() - t0) / pcg_sample
+    t_step = t4 + t2l + t2r + iters * t_it
+    sample = ("element loops isw4/isw2(lhs)/isw2(rhs) on %d of %d elements scaled to the mesh, "
+              "%d PCG iterations scaled to the step's %d; %d threads" % (S, numel, pcg_sample,
+                                                                         iters, threads))
+    return t_step, dict(t_isw4=t4, t_isw2_lhs=t2l, t_isw2_rhs=t2r, t_pcg_iter=t_it), sample, threads
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from poromec_gb300 import meshgen
+    pb = meshgen.cube_problem(args.n)
+    iters = int(os.environ.get("PM_REF_ITERS", "0")) or 2500
+    times = []
+    for k in range(args.warmup + args.steps):
+        t_step, parts, sample, threads = cpu_step_estimate(pb, iters, elem_sample=200,
+                                                           pcg_sample=2)
+        if k >= args.warmup:
+            times.append(t_step)
+    v = 1.0 / statistics.mean(times)
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "heterogeneous cube, hexa20 %d^3, PCG tol %g" % (
+               args.n, args.solvtol), "pcg_iterations_per_step": iters},
+           "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    import poromec_gb300 as pg
+    from poromec_gb300 import meshgen
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    pb = meshgen.cube_problem(args.n)
+    m = pg.from_problem(pb)
+    step_kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=args.solvtol,
+                   maxit=200000, reassemble=True)
+    for _ in range(args.warmup):
+        m.step(**step_kw)
+    snap = m.get_state()
+    barrier()
+    iters = []
+    timers = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            info = m.step(**step_kw)
+            iters.append(info.iters)
+            timers.append(m.timers())
+        barrier()
+        elapsed = time.perf_counter() - t0
+    u64, _, _ = m.get_state()
+    ms = elapsed / args.steps * 1e3
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps / elapsed
+
+    # e2e: the same step through the C ABI with the nodal state in pinned host
+    # memory, copied in before and out after every step.
+    u_h, u0_h, dp_h = [torch.from_numpy(a.copy()).pin_memory().numpy() for a in snap]
+    m.set_state(*snap)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        m.set_state(u_h, u0_h, dp_h)
+        m.step(**step_kw)
+        u_o, u0_o, dp_o = m.get_state()
+        u_h[...], u0_h[...], dp_h[...] = u_o, u0_o, dp_o
+    barrier()
+    e2e_elapsed = time.perf_counter() - t0
+    nbytes = u_h.nbytes + u0_h.nbytes + dp_h.nbytes
+
+    # FP32 values + FP64 refinement from the same state
+    mixed = None
+    if not args.no_mixed:
+        m.set_state(*snap)
+        m.set_precision(pg.capi.PM_FP32_REFINE)
+        barrier()
+        t0 = time.perf_counter()
+        mi = []
+        for _ in range(args.steps):
+            info = m.step(**step_kw)
+            mi.append((info.iters, info.refine))
+        barrier()
+        t_mixed = time.perf_counter() - t0
+        u32, _, _ = m.get_state()
+        m.set_precision(pg.capi.PM_FP64)
+        err_u = float(np.abs(u32[:, :3] - u64[:, :3]).max() / np.abs(u64[:, :3]).max())
+        err_p = float(np.abs(u32[:, 3] - u64[:, 3]).max() / np.abs(u64[:, 3]).max())
+        mixed = {"value": world * args.steps / t_mixed, "unit": "steps/s",
+                 "speedup_vs_fp64": (args.steps / t_mixed) / (args.steps / (elapsed)),
+                 "rel_err_u": err_u, "rel_err_p": err_p,
+                 "inner_iterations_per_step": [a for a, _ in mi],
+                 "refine_sweeps_per_step": [b for _, b in mi]}
+
+    # SpMV roofline: the dominant kernel timed alone with CUDA events on the
+    # stream it is launched on, 50 launches over the assembled matrix
+    x = torch.randn(m.neq, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    s = torch.cuda.current_stream()
+    for _ in range(5):
+        m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nl = 50
+    e0.record(s)
+    for _ in range(nl):
+        m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / nl
+    B = spmv_bytes(m.nad, m.neq)
+    achieved = B / (spmv_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    traffic = profile_traffic(m.nnz_panel)
+    tm = np.mean(np.array(timers), 0)
+
+    if rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian random fields, structured mesh)",
+        "config": {"workload": "heterogeneous cube, hexa20 %d^3, %d equations, nad %d, "
+                               "PCG tol %g, K re-assembled every step" % (
+                                   args.n, m.neq, m.nad, args.solvtol),
+                   "l2": "inputs larger than L2 (panel values %.2f GB)" % (m.nnz_panel * 8e-9),
+                   "pcg_iterations_per_step": iters,
+                   "phase_ms": {"pload_isw4": tm[0], "assembly_isw2": tm[1],
+                                "residual_isw2": tm[2], "solve": tm[3]},
+                   "replicas": world},
+        "e2e": {"value": world * args.steps / e2e_elapsed, "unit": "steps/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "spmv_gbs": achieved,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
+                     "kernel": "k_spmv<double> (node panels)", "launch_ms": spmv_ms,
+                     "algorithmic_bytes": B, "traffic": traffic},
+        "gpu_launches": int(round(args.steps * tm[7])),
+        "clocks": clk.summary(),
+    }
+    if mixed:
+        out["fp32_refine"] = mixed
+    if not args.no_cpu:
+        t_step, parts, sample, threads = cpu_step_estimate(pb, int(np.mean(iters)))
+        out["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads,
+                               "kind": "port", "sample": sample,
+                               "parts_s": {k: round(v, 4) for k, v in parts.items()}}
+    print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

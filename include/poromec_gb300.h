@@ -146,7 +146,7 @@ int pm_matvec_csrd_dev(int neq, const int64_t* d_ia, const int32_t* d_ja,
 /* Timing of the last pm_step phases in milliseconds (CUDA events):
  * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,
  * [3] solve, [4] updates, [5] SpMV kernel time of the solve (sum),
- * [6] number of SpMV launches in the solve. */
+ * [6] Krylov iterations of the last solve, [7] kernels launched by the step. */
 int pm_get_timers(pm_handle h, double* t, int n);
 
 #ifdef __cplusplus

@@ -167,6 +167,12 @@ class Oracle:
                "or_pform")
         return b
 
+    def pform_range(self, isw, lhs, rhs, u, b, nthreads, e_begin, e_end):
+        ua = _f64(u)
+        _check(lib().or_pform_range(self.h, isw, int(lhs), int(rhs), _p(ua), _p(b), nthreads,
+                                    e_begin, e_end), "or_pform_range")
+        return b
+
     def matvec(self, x, nthreads=1):
         xa = _f64(x)
         y = np.zeros(self.neq)

@@ -1079,8 +1079,10 @@ int element_type_ok(const or_handle_s* h, int nel) {
 }
 
 int pform(or_handle_s* h, int isw, bool lhs, bool rhs, const double* u,
-          double* b, int nthreads, const double* tx0) {
-  if (lhs) {
+          double* b, int nthreads, const double* tx0, int e_begin = 1,
+          int e_end = -1, bool zero = true) {
+  if (e_end < 0) e_end = h->numel + 1;
+  if (lhs && zero) {
     std::fill(h->al.begin(), h->al.end(), 0.0);
     std::fill(h->ad.begin(), h->ad.end(), 0.0);
   }
@@ -1104,7 +1106,7 @@ int pform(or_handle_s* h, int isw, bool lhs, bool rhs, const double* u,
   };
   if (nthreads <= 1) {
     std::vector<double> s((size_t)nst * nst), p(nst);
-    for (int nel = 1; nel <= h->numel; ++nel) {
+    for (int nel = e_begin; nel < e_end; ++nel) {
       const int st = body(nel, s, p);
       if (st != OR_OK) return st;
     }
@@ -1115,7 +1117,9 @@ int pform(or_handle_s* h, int isw, bool lhs, bool rhs, const double* u,
       for (int c = 0; c < h->numcolors; ++c) {
 #pragma omp for schedule(static)
         for (int jc = h->color_ptr[c]; jc < h->color_ptr[c + 1]; ++jc) {
-          const int st = body(h->color_elems[jc], s, p);
+          const int nel = h->color_elems[jc];
+          if (nel < e_begin || nel >= e_end) continue;
+          const int st = body(nel, s, p);
           if (st != OR_OK) {
 #pragma omp critical
             status = st;
@@ -1574,6 +1578,14 @@ int or_pform(or_handle h, int isw, int lhs, int rhs, const double* u, double* b,
              int nthreads) {
   if (!h || !u || !b) return OR_E_ARG;
   return pform(h, isw, lhs != 0, rhs != 0, u, b, nthreads, nullptr);
+}
+
+int or_pform_range(or_handle h, int isw, int lhs, int rhs, const double* u,
+                   double* b, int nthreads, int e_begin, int e_end) {
+  if (!h || !u || !b || e_begin < 1 || e_end > h->numel + 1 || e_begin > e_end)
+    return OR_E_ARG;
+  // a timing sample of the element loop: ad/al are not zeroed first
+  return pform(h, isw, lhs != 0, rhs != 0, u, b, nthreads, nullptr, e_begin, e_end, false);
 }
 
 int or_matvec(or_handle h, const double* x, double* y, int nthreads) {

@@ -81,6 +81,11 @@ int or_element(or_handle h, int nel, int isw, const double* ul,
 int or_pform(or_handle h, int isw, int lhs, int rhs, const double* u,
              double* b, int nthreads);
 
+/* The element loop of or_pform restricted to elements [e_begin, e_end)
+ * (1-based), without zeroing ad/al: a bounded timing sample of pform_pm. */
+int or_pform_range(or_handle h, int isw, int lhs, int rhs, const double* u,
+                   double* b, int nthreads, int e_begin, int e_end);
+
 /* matvec_csrc_sym_pm (Matvec.f:1504-1598); nthreads > 1 runs the
  * row-partitioned variant with per-thread buffers (Matvec_omp.f:461-587). */
 int or_matvec(or_handle h, const double* x, double* y, int nthreads);

@@ -187,6 +187,7 @@ int assemble_K(Handle* h, bool fp32) {
   } else {
     PM_CUDA(cudaMemsetAsync(h->P.val, 0, sizeof(double) * (size_t)h->P.nnz, h->stream));
   }
+  h->launches += h->numcolors;
   for (int c = 0; c < h->numcolors; ++c)
     PM_CUDA(pm::launch_assemble_K(elem_launch(h, c), h->hexa, fp32 ? nullptr : h->P.val,
                                   fp32 ? h->P.val32 : nullptr, h->stream));
@@ -197,12 +198,14 @@ int assemble_K(Handle* h, bool fp32) {
 }
 
 int residual(Handle* h, const double* du, double* b) {
+  h->launches += h->numcolors;
   for (int c = 0; c < h->numcolors; ++c)
     PM_CUDA(pm::launch_residual(elem_launch(h, c), h->hexa, du, b, h->stream));
   return PM_OK;
 }
 
 int rhs4(Handle* h, const double* u, double* b) {
+  h->launches += h->numcolors;
   for (int c = 0; c < h->numcolors; ++c)
     PM_CUDA(pm::launch_rhs4(elem_launch(h, c), h->hexa, u, h->D.dp, h->D.eload, h->D.eloadp,
                             h->D.load, h->D.fload, h->maxt, b, h->stream));
@@ -215,6 +218,7 @@ int build_precond(Handle* h, int precond) {
     h->err = "precond must be 2 (diag) or 5 (|diag|)";
     return PM_E_ARG;
   }
+  h->launches += 2;
   PM_CUDA(pm::panel_diag(h->P.view(), h->P.val, nullptr, h->D.ad, h->stream));
   PM_CUDA(cudaMemsetAsync(h->D.err, 0, sizeof(int), h->stream));
   PM_CUDA(pm::precond(h->neq, h->D.ad, h->D.m, precond == 5, h->D.err, h->stream));
@@ -282,10 +286,12 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       }));
       h->pcg_graph_val = vkey;
     }
+    h->launches += 1;
     PM_CUDA(pm::pcg_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
                          h->stream));
     for (;;) {
       PM_CUDA(cudaGraphLaunch(h->pcg_graph, h->stream));
+      h->launches += 3 * kGraphIters;
       PM_TRY(read_scalars(h, &ks));
       if (ks.conv_flag) break;
     }
@@ -312,11 +318,13 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     int nrestart = 10;  // call_minres, Solv.f:1727
     bool zero_x = true;
     for (;;) {
+      h->launches += zero_x ? 1 : 2;
       PM_CUDA(pm::minres_start(P, val64, val32, n, d_b, h->D.m, V, h->D.ks, maxit, zero_x,
                                h->D.partial, h->D.counter, h->stream));
       zero_x = false;
       for (;;) {
         PM_CUDA(cudaGraphLaunch(h->minres_graph, h->stream));
+        h->launches += 3 * kGraphIters;
         PM_TRY(read_scalars(h, &ks));
         if (ks.conv_flag) break;
       }
@@ -340,6 +348,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   }
   PM_CUDA(cudaEventRecord(e1, h->stream));
   // x.Kx of the solver log (one more product with the converged x)
+  h->launches += 1;
   PM_CUDA(pm::spmv(P, val64, val32, V.x, V.q, 3, h->D.ks, h->D.partial, h->D.counter,
                    h->stream));
   if (d_x != V.x)
@@ -374,6 +383,7 @@ int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   for (sweep = 0; sweep < 60; ++sweep) {
     // ||r||_|M| = sqrt(sum |m_i| r_i^2), a norm also on the indefinite system
     double rn2 = 0.0;
+    h->launches += 1;
     PM_CUDA(pm::wnorm2(n, r, h->D.m, h->D.norms, h->D.partial, h->D.counter, h->stream));
     PM_CUDA(cudaMemcpyAsync(&rn2, h->D.norms, sizeof(double), cudaMemcpyDeviceToHost,
                             h->stream));
@@ -387,6 +397,7 @@ int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     const double itol = std::max(h->inner_tol, 0.5 * tol * bnorm / rn);
     PM_TRY(krylov(h, solver, r, dx, itol, maxit, h->P.val32, &in));
     total += in.iters;
+    h->launches += 3;
     PM_CUDA(pm::axpy_into(n, d_x, dx, 1.0, h->stream));
     // r = b - A64 x  (FP64 panels)
     PM_CUDA(pm::spmv(P, h->P.val, nullptr, d_x, h->D.by, 0, nullptr, nullptr, nullptr,
@@ -413,6 +424,7 @@ int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x
       if (!h->P.val32) {
         PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
       }
+      h->launches += 1;
       PM_CUDA(pm::to_f32(h->P.nnz, h->P.val, h->P.val32, h->stream));
       h->assembled32 = true;
     }
@@ -825,9 +837,11 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
       for (int i = 0; i < 6; ++i) cudaEventDestroy(e[i]);
     }
   } guard{ev};
+  const int64_t launches0 = h->launches;
   h->istep += 1;
   h->t = h->t + h->dt;
   PM_CUDA(cudaEventRecord(ev[0], s));
+  h->launches += 2 + (h->fstress0 ? 1 : 0);  // pload, predict, initial stress
   k_pload<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.nload, D.f, D.u, D.b0,
                                               D.load, D.fload, h->maxt, D.x, h->t, h->dt,
                                               h->gravity_mod);
@@ -859,6 +873,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
     cudaEventElapsedTime(&ms, ev[3], ev[4]);
     t_res += ms;
     if (stop_crit == 1 || stop_crit == 2) {
+      h->launches += 1;
       PM_CUDA(pm::resnorms(h->neq, D.b, D.dofkind, D.norms, D.partial, D.counter, s));
       double nr[2];
       PM_CUDA(cudaMemcpyAsync(nr, D.norms, sizeof(nr), cudaMemcpyDeviceToHost, s));
@@ -895,6 +910,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
     loc.refine = si.refine;
     loc.conv = si.conv;
     loc.xkx = si.xkx;
+    h->launches += 1;
     k_delta_update<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.u, D.xs);
     PM_CUDA(cudaGetLastError());
     PM_CUDA(cudaEventSynchronize(ev[3]));
@@ -918,6 +934,8 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   h->timers[1] = t_asm;
   h->timers[2] = t_res;
   h->timers[3] = t_sol;
+  h->launches += 1;  // update_res
+  h->timers[7] = (double)(h->launches - launches0);
   if (info) *info = loc;
   return PM_OK;
 }

@@ -147,6 +147,7 @@ struct Handle {
   const void* minres_graph_val = nullptr;
   const double* pcg_graph_m = nullptr;
   double timers[8] = {0};
+  int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;
 };
 
