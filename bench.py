@@ -233,6 +233,12 @@ def run_gpu(args):
     for _ in range(args.warmup):
         m.step(**step_kw)
     snap = m.get_state()
+    t_snap = args.warmup * float(pb["dt"])
+
+    def restore():
+        # state and clock of the first timed step (the top load ramps in time)
+        m.set_state(*snap)
+        m.set_env(pb["gravity"], float(pb["dt"]), t_snap, args.warmup)
     barrier()
     iters = []
     timers = []
@@ -255,7 +261,7 @@ def run_gpu(args):
     # e2e: the same step through the C ABI with the nodal state in pinned host
     # memory, copied in before and out after every step.
     u_h, u0_h, dp_h = [torch.from_numpy(a.copy()).pin_memory().numpy() for a in snap]
-    m.set_state(*snap)
+    restore()
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -270,7 +276,7 @@ def run_gpu(args):
     # FP32 values + FP64 refinement from the same state
     mixed = None
     if not args.no_mixed:
-        m.set_state(*snap)
+        restore()
         m.set_precision(pg.capi.PM_FP32_REFINE)
         barrier()
         t0 = time.perf_counter()
@@ -294,9 +300,10 @@ def run_gpu(args):
     # stream it is launched on, 50 launches over the assembled matrix
     x = torch.randn(m.neq, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
-    s = torch.cuda.current_stream()
+    s = torch.cuda.Stream()  # a real stream handle (0 would select the library's own)
     for _ in range(5):
         m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     nl = 50
     e0.record(s)

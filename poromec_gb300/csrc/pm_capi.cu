@@ -182,6 +182,10 @@ int assemble_K(Handle* h, bool fp32) {
     if (!h->P.val32) {
       PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
       h->pcg_graph_val = h->minres_graph_val = nullptr;
+      if (h->pcg32_graph) {
+        cudaGraphExecDestroy(h->pcg32_graph);
+        h->pcg32_graph = nullptr;
+      }
     }
     PM_CUDA(cudaMemsetAsync(h->P.val32, 0, sizeof(float) * (size_t)h->P.nnz, h->stream));
   } else {
@@ -273,7 +277,10 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   const int n = h->neq;
   pm::KrylovVecs& V = h->D.kv;
   const pm::PanelView P = h->P.view();
-  const double* val64 = val32 ? nullptr : h->P.val;
+  // the FP64 solve runs on the FP64 panels; the FP32 operator has its own
+  // inner solver (refine)
+  const double* val64 = h->P.val;
+  val32 = nullptr;
   pm::KrylovScalars ks{};
   cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
   PM_CUDA(cudaEventRecord(e0, h->stream));
@@ -366,20 +373,33 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   return PM_OK;
 }
 
-// FP64 iterative refinement around an FP32-valued Krylov solve:
-// x = 0; repeat r = b - A64 x (FP64), solve A32 dx = r loosely, x += dx
-// until ||r||_M <= tol ||b||_M.  Residuals, dot products, norms and the
-// diagonal stay FP64.
+// FP64 iterative refinement around an FP32 PCG:
+// x = 0; repeat r = b - A64 x (FP64 panels, FP64 arithmetic), solve
+// A32 dx = r with PCG on FP32 values and FP32 vectors to a loose relative
+// tolerance, x += dx; stop when ||r||_|M| <= tol ||b||_|M|.  Residuals, the
+// norms and the diagonal preconditioner stay FP64.
 int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, int maxit,
            pm_step_info* info) {
+  if (solver != 1) {
+    h->err = "FP32 refinement is implemented for PCG (solver 1)";
+    return PM_E_ARG;
+  }
   const int n = h->neq;
   const pm::PanelView P = h->P.view();
   double* r = h->D.rr;
-  double* dx = h->D.dx;
+  pm::KrylovVecs32& V = h->D.kv32;
   PM_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, h->stream));
   PM_CUDA(cudaMemcpyAsync(r, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  if (!h->pcg32_graph) {
+    PM_TRY(capture(h, &h->pcg32_graph, [&]() {
+      return pm::pcg32_iteration(P, h->P.val32, n, V, h->D.ks, h->D.partial, h->D.counter,
+                                 h->stream);
+    }));
+  }
   double bnorm = -1.0;
   int total = 0, sweep = 0;
+  cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
+  PM_CUDA(cudaEventRecord(e0, h->stream));
   for (sweep = 0; sweep < 60; ++sweep) {
     // ||r||_|M| = sqrt(sum |m_i| r_i^2), a norm also on the indefinite system
     double rn2 = 0.0;
@@ -391,19 +411,41 @@ int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     const double rn = std::sqrt(rn2);
     if (bnorm < 0) bnorm = rn;
     if (rn <= tol * bnorm || rn == 0.0) break;
-    pm_step_info in{};
     // inner tolerance relative to the current residual, never tighter than
     // needed for the outer target
     const double itol = std::max(h->inner_tol, 0.5 * tol * bnorm / rn);
-    PM_TRY(krylov(h, solver, r, dx, itol, maxit, h->P.val32, &in));
-    total += in.iters;
+    pm::KrylovScalars ks{};
+    h->launches += 1;
+    PM_CUDA(pm::pcg32_init(n, r, h->D.m, V, h->D.ks, itol, maxit, h->D.partial, h->D.counter,
+                           h->stream));
+    for (;;) {
+      PM_CUDA(cudaGraphLaunch(h->pcg32_graph, h->stream));
+      h->launches += 3 * kGraphIters;
+      PM_TRY(read_scalars(h, &ks));
+      if (ks.conv_flag) break;
+    }
+    if (ks.conv_flag == 3) {
+      h->err = "refinement: inner PCG breakdown";
+      return PM_E_NOCONV;
+    }
+    total += ks.iter;
+    // x += dx;  r = b - A64 x
     h->launches += 3;
-    PM_CUDA(pm::axpy_into(n, d_x, dx, 1.0, h->stream));
-    // r = b - A64 x  (FP64 panels)
+    PM_CUDA(pm::add_f32(n, d_x, V.x, h->stream));
     PM_CUDA(pm::spmv(P, h->P.val, nullptr, d_x, h->D.by, 0, nullptr, nullptr, nullptr,
                      h->stream));
     PM_CUDA(pm::vsub(n, r, d_b, h->D.by, h->stream));
   }
+  if (sweep == 60) {
+    h->err = "refinement: no convergence after 60 sweeps";
+    return PM_E_NOCONV;
+  }
+  PM_CUDA(cudaEventRecord(e1, h->stream));
+  PM_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  h->timers[5] = ms;
+  h->timers[6] = total;
   if (info) {
     info->iters = total;
     info->refine = sweep;
@@ -423,6 +465,10 @@ int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x
     if (!h->assembled32) {
       if (!h->P.val32) {
         PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
+        if (h->pcg32_graph) {
+          cudaGraphExecDestroy(h->pcg32_graph);
+          h->pcg32_graph = nullptr;
+        }
       }
       h->launches += 1;
       PM_CUDA(pm::to_f32(h->P.nnz, h->P.val, h->P.val32, h->stream));
@@ -463,6 +509,14 @@ int alloc_state(Handle* h) {
     PM_TRY(A(p, n));
   PM_CUDA(cudaMalloc(&D.ks, sizeof(pm::KrylovScalars)));
   PM_CUDA(cudaMemset(D.ks, 0, sizeof(pm::KrylovScalars)));
+  pm::KrylovVecs32& V32 = D.kv32;
+  for (float** p : {&V32.x, &V32.r, &V32.z, &V32.p, &V32.q, &V32.m}) {
+    if (cudaMalloc((void**)p, sizeof(float) * std::max<size_t>(n, 1)) != cudaSuccess) {
+      h->err = "cudaMalloc failed";
+      return PM_E_NOMEM;
+    }
+    cudaMemset(*p, 0, sizeof(float) * std::max<size_t>(n, 1));
+  }
   PM_TRY(A(&D.partial, 4 * (size_t)pm::kRedBlocks));
   PM_CUDA(cudaMalloc(&D.counter, sizeof(unsigned) * 4));
   PM_CUDA(cudaMemset(D.counter, 0, sizeof(unsigned) * 4));
@@ -483,7 +537,11 @@ void free_all(Handle* h) {
                   P.val32, P.node_val_off, P.node_W};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (void* p : {(void*)D.kv32.x, (void*)D.kv32.r, (void*)D.kv32.z, (void*)D.kv32.p,
+                  (void*)D.kv32.q, (void*)D.kv32.m})
+    if (p) cudaFree(p);
   if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
+  if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);

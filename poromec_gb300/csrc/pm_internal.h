@@ -104,6 +104,7 @@ struct Dev {
   double *rr = nullptr, *dx = nullptr;   // refinement residual / correction
   double* xs = nullptr;                  // solution of the step's solve
   KrylovVecs kv{};
+  KrylovVecs32 kv32{};
   KrylovScalars* ks = nullptr;
   double* partial = nullptr;
   unsigned* counter = nullptr;
@@ -142,7 +143,7 @@ struct Handle {
   Dev D;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
-  cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr;
+  cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr, pcg32_graph = nullptr;
   const void* pcg_graph_val = nullptr;   // values pointer baked into the graph
   const void* minres_graph_val = nullptr;
   const double* pcg_graph_m = nullptr;

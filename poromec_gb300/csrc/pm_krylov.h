@@ -39,7 +39,21 @@ struct KrylovVecs {
   double *v, *v0, *w0, *w00, *z0;   // MINRES (also uses x, z, p, q)
 };
 
+// FP32 vectors of the refinement's inner PCG.
+struct KrylovVecs32 {
+  float *x, *r, *z, *p, *q, *m;
+};
+
 int vec_grid(int n);
+cudaError_t spmv32(const PanelView& P, const float* val32, const float* x, float* y, int mode,
+                   KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t pcg32_init(int n, const double* b, const double* m, KrylovVecs32& V,
+                       KrylovScalars* ks, double tol, int maxit, double* partial,
+                       unsigned* counter, cudaStream_t s);
+cudaError_t pcg32_iteration(const PanelView& P, const float* val32, int n, KrylovVecs32& V,
+                            KrylovScalars* ks, double* partial, unsigned* counter,
+                            cudaStream_t s);
+cudaError_t add_f32(int n, double* y, const float* x, cudaStream_t s);
 cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
                  const double* x, double* y, int mode, KrylovScalars* ks,
                  double* partial, unsigned* counter, cudaStream_t s);

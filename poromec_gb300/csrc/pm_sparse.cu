@@ -84,60 +84,86 @@ __device__ __forceinline__ bool krylov_skip(KrylovScalars* ks, bool first) {
 }
 
 // ---- SpMV over panels ------------------------------------------------------
+// A sub-warp of 8 lanes per node: lane t of the sub-warp accumulates columns
+// t, t+8, ... of the node's d <= 4 panel rows (coalesced 64-byte runs per
+// row), then the 4 row sums are reduced across the 8 lanes with a
+// transposed butterfly (each lane keeps half of its values at every level:
+// 4 adds per lane instead of 4 x 3).  On GB300 the FP64 pipe issues 2
+// DFMA per clock per SM, so for T = double the kernel is bound by FP64
+// instructions, not HBM: the count is one FMA per stored value plus 4 adds
+// per lane and node.  T = float is the FP32 inner operator of the refinement.
+//
 // MODE 0: y = A x.   MODE 1: PCG, also alpha = d / (y . x).
 // MODE 2: MINRES, also alpha = |x . y| / beta^2.   MODE 3: y = A x and
 // ks->xkx = x . y (energy norm of the solver log).
-template <typename TV, int MODE>
+constexpr int kSub = 8;
+
+template <typename T>
+__device__ __forceinline__ T shfl(T v, int m) {
+  return __shfl_xor_sync(0xffffffffu, v, m);
+}
+
+template <typename T, int MODE>
 __global__ void __launch_bounds__(256)
-    k_spmv(PanelView P, const TV* __restrict__ val, const double* __restrict__ x,
-           double* __restrict__ y, KrylovScalars* ks, double* partial,
-           unsigned* counter) {
+    k_spmv(PanelView P, const T* __restrict__ val, const T* __restrict__ x,
+           T* __restrict__ y, KrylovScalars* ks, double* partial, unsigned* counter) {
   if (MODE == 1 || MODE == 2)
     if (krylov_skip(ks, true)) return;
   const int lane = threadIdx.x & 31;
-  const int wid = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nw = (int)((gridDim.x * blockDim.x) >> 5);
-  double dsum = 0.0;
-  for (int node = wid; node < P.nact; node += nw) {
-    const int e0 = P.eq0[node], d = P.d[node], W = P.W[node];
-    const TV* v = val + P.val_off[node];
-    const int32_t* cols = P.cols + P.col_off[node];
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    if (d == 4) {
-      for (int c = lane; c < W; c += 32) {
-        const double xv = x[cols[c]];
-        a0 += double(v[c]) * xv;
-        a1 += double(v[W + c]) * xv;
-        a2 += double(v[2 * W + c]) * xv;
-        a3 += double(v[3 * W + c]) * xv;
-      }
-    } else if (d == 3) {
-      for (int c = lane; c < W; c += 32) {
-        const double xv = x[cols[c]];
-        a0 += double(v[c]) * xv;
-        a1 += double(v[W + c]) * xv;
-        a2 += double(v[2 * W + c]) * xv;
-      }
-    } else {
-      for (int c = lane; c < W; c += 32) {
-        const double xv = x[cols[c]];
-        a0 += double(v[c]) * xv;
-        if (d > 1) a1 += double(v[W + c]) * xv;
-        if (d > 2) a2 += double(v[2 * W + c]) * xv;
+  const int t = lane & (kSub - 1);
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
+  constexpr int kNodesPerWarp = 32 / kSub;
+  T dsum = T(0);
+  for (int base = warp * kNodesPerWarp; base < P.nact; base += nwarp * kNodesPerWarp) {
+    const int node = base + (lane >> 3);
+    int e0 = 0, d = 0, W = 0;
+    T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+    if (node < P.nact) {
+      e0 = P.eq0[node];
+      d = P.d[node];
+      W = P.W[node];
+      const T* v = val + P.val_off[node];
+      const int32_t* cols = P.cols + P.col_off[node];
+      if (d == 4) {
+        for (int c = t; c < W; c += kSub) {
+          const T xv = x[cols[c]];
+          a0 += v[c] * xv;
+          a1 += v[W + c] * xv;
+          a2 += v[2 * W + c] * xv;
+          a3 += v[3 * W + c] * xv;
+        }
+      } else if (d == 3) {
+        for (int c = t; c < W; c += kSub) {
+          const T xv = x[cols[c]];
+          a0 += v[c] * xv;
+          a1 += v[W + c] * xv;
+          a2 += v[2 * W + c] * xv;
+        }
+      } else {
+        for (int c = t; c < W; c += kSub) {
+          const T xv = x[cols[c]];
+          a0 += v[c] * xv;
+          if (d > 1) a1 += v[W + c] * xv;
+        }
       }
     }
-    a0 = warp_sum(a0);
-    if (d > 1) a1 = warp_sum(a1);
-    if (d > 2) a2 = warp_sum(a2);
-    if (d > 3) a3 = warp_sum(a3);
-    if (lane < d) {
-      const double yv = lane == 0 ? a0 : lane == 1 ? a1 : lane == 2 ? a2 : a3;
-      y[e0 + lane] = yv;
-      if (MODE != 0) dsum += yv * x[e0 + lane];
+    // transposed butterfly over the 8 lanes of the sub-warp
+    const bool h4 = (t & 4) != 0, h2 = (t & 2) != 0;
+    T k0 = h4 ? a2 : a0, k1 = h4 ? a3 : a1;
+    k0 += shfl(h4 ? a0 : a2, 4);
+    k1 += shfl(h4 ? a1 : a3, 4);
+    T k = h2 ? k1 : k0;
+    k += shfl(h2 ? k0 : k1, 2);
+    k += shfl(k, 1);
+    const int r = (h4 ? 2 : 0) + (h2 ? 1 : 0);
+    if ((t & 1) == 0 && r < d) {
+      y[e0 + r] = k;
+      if (MODE != 0) dsum += k * x[e0 + r];
     }
   }
   if (MODE != 0) {
-    double in[1] = {dsum}, tot[1];
+    double in[1] = {double(dsum)}, tot[1];
     if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
       if (MODE == 1) {
         ks->pq = tot[0];
@@ -217,6 +243,79 @@ __global__ void __launch_bounds__(256)
   const double beta = ks->beta;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     p[i] = z[i] + beta * p[i];
+}
+
+// ---- FP32 inner PCG of the refinement --------------------------------------
+// The same recurrences on FP32 vectors and the FP32 panel values; dot
+// products accumulate per thread in FP32 and across threads in FP64.
+__global__ void __launch_bounds__(256)
+    k_pcg32_init(int n, const double* __restrict__ b, const double* __restrict__ m,
+                 float* __restrict__ m32, float* __restrict__ r, float* __restrict__ z,
+                 float* __restrict__ p, float* __restrict__ x, KrylovScalars* ks, double tol,
+                 int maxit, double* partial, unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float mi = float(m[i]);
+    const float bi = float(b[i]), zi = bi * mi;
+    m32[i] = mi;
+    x[i] = 0.f;
+    r[i] = bi;
+    z[i] = zi;
+    p[i] = zi;
+    acc += double(bi * zi);
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    ks->d = tot[0];
+    ks->bmb = tot[0];
+    ks->conv = tol * sqrt(fabs(tot[0]));
+    ks->done = 0;
+    ks->conv_flag = 0;
+    ks->iter = 0;
+    ks->maxit = maxit;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_pcg32_update(int n, float* __restrict__ x, const float* __restrict__ p,
+                   float* __restrict__ r, const float* __restrict__ q,
+                   const float* __restrict__ m, float* __restrict__ z, KrylovScalars* ks,
+                   double* partial, unsigned* counter) {
+  if (krylov_skip(ks, false)) return;
+  const float alpha = float(ks->alpha);
+  float acc = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] = x[i] + alpha * p[i];
+    const float ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    const float zi = ri * m[i];
+    z[i] = zi;
+    acc += ri * zi;
+  }
+  double in[1] = {double(acc)}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    const double di = tot[0];
+    ks->beta = di / ks->d;
+    ks->d = di;
+    ks->iter += 1;
+    if (sqrt(fabs(di)) < ks->conv) ks->conv_flag = 1;
+    else if (!isfinite(di)) ks->conv_flag = 3;
+    else if (ks->iter >= ks->maxit) ks->conv_flag = 2;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_pcg32_dir(int n, const float* __restrict__ z, float* __restrict__ p, KrylovScalars* ks) {
+  if (krylov_skip(ks, false)) return;
+  const float beta = float(ks->beta);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+// x64 += double(x32)
+__global__ void k_add_f32(int n, double* __restrict__ y, const float* __restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] += double(x[i]);
 }
 
 // ---- MINRES ----------------------------------------------------------------
@@ -478,22 +577,46 @@ int vec_grid(int n) {
 cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
                  const double* x, double* y, int mode, KrylovScalars* ks,
                  double* partial, unsigned* counter, cudaStream_t s) {
+  (void)val32;  // the FP32 operator runs on FP32 vectors: spmv32
   const int grid = kRedBlocks;
-  if (val32) {
-    switch (mode) {
-      case 0: k_spmv<float, 0><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
-      case 1: k_spmv<float, 1><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
-      case 2: k_spmv<float, 2><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
-      default: k_spmv<float, 3><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter); break;
-    }
-  } else {
-    switch (mode) {
-      case 0: k_spmv<double, 0><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
-      case 1: k_spmv<double, 1><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
-      case 2: k_spmv<double, 2><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
-      default: k_spmv<double, 3><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
-    }
+  switch (mode) {
+    case 0: k_spmv<double, 0><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+    case 1: k_spmv<double, 1><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+    case 2: k_spmv<double, 2><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
+    default: k_spmv<double, 3><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t spmv32(const PanelView& P, const float* val32, const float* x, float* y, int mode,
+                   KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s) {
+  const int grid = kRedBlocks;
+  if (mode == 0) k_spmv<float, 0><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter);
+  else k_spmv<float, 1><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t pcg32_init(int n, const double* b, const double* m, KrylovVecs32& V,
+                       KrylovScalars* ks, double tol, int maxit, double* partial,
+                       unsigned* counter, cudaStream_t s) {
+  k_pcg32_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.m, V.r, V.z, V.p, V.x, ks, tol, maxit,
+                                            partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t pcg32_iteration(const PanelView& P, const float* val32, int n, KrylovVecs32& V,
+                            KrylovScalars* ks, double* partial, unsigned* counter,
+                            cudaStream_t s) {
+  cudaError_t e = spmv32(P, val32, V.p, V.q, 1, ks, partial, counter, s);
+  if (e != cudaSuccess) return e;
+  k_pcg32_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, V.m, V.z, ks, partial,
+                                              counter);
+  k_pcg32_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t add_f32(int n, double* y, const float* x, cudaStream_t s) {
+  k_add_f32<<<vec_grid(n), 256, 0, s>>>(n, y, x);
   return cudaGetLastError();
 }
 
