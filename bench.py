@@ -39,7 +39,7 @@ METRIC = "Biot steps/s at 2M dof: FP64 plain vs FP32+refine at 1e-8 rel; SpMV HB
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=56, help="elements per cube edge")
@@ -273,11 +273,23 @@ def run_gpu(args):
     e2e_elapsed = time.perf_counter() - t0
     nbytes = u_h.nbytes + u0_h.nbytes + dp_h.nbytes
 
+    # Accuracy reference: the same steps in FP64 at tolerance 1e-12 (untimed).
+    restore()
+    for _ in range(args.steps):
+        m.step(**dict(step_kw, solvtol=1e-12))
+    u_ref, _, _ = m.get_state()
+
+    def rel_err(a):
+        eu = float(np.abs(a[:, :3] - u_ref[:, :3]).max() / np.abs(u_ref[:, :3]).max())
+        ep = float(np.abs(a[:, 3] - u_ref[:, 3]).max() / np.abs(u_ref[:, 3]).max())
+        return eu, ep
+
     # FP32 values + FP64 refinement from the same state
     mixed = None
     if not args.no_mixed:
         restore()
         m.set_precision(pg.capi.PM_FP32_REFINE)
+        m.set_refine(1e-5)
         barrier()
         t0 = time.perf_counter()
         mi = []
@@ -288,13 +300,13 @@ def run_gpu(args):
         t_mixed = time.perf_counter() - t0
         u32, _, _ = m.get_state()
         m.set_precision(pg.capi.PM_FP64)
-        err_u = float(np.abs(u32[:, :3] - u64[:, :3]).max() / np.abs(u64[:, :3]).max())
-        err_p = float(np.abs(u32[:, 3] - u64[:, 3]).max() / np.abs(u64[:, 3]).max())
+        eu, ep = rel_err(u32)
         mixed = {"value": world * args.steps / t_mixed, "unit": "steps/s",
-                 "speedup_vs_fp64": (args.steps / t_mixed) / (args.steps / (elapsed)),
-                 "rel_err_u": err_u, "rel_err_p": err_p,
+                 "speedup_vs_fp64": (args.steps / t_mixed) / (args.steps / elapsed),
+                 "rel_err_u_vs_fp64_1e-12": eu, "rel_err_p_vs_fp64_1e-12": ep,
                  "inner_iterations_per_step": [a for a, _ in mi],
                  "refine_sweeps_per_step": [b for _, b in mi]}
+    eu64, ep64 = rel_err(u64)
 
     # SpMV roofline: the dominant kernel timed alone with CUDA events on the
     # stream it is launched on, 50 launches over the assembled matrix
@@ -336,6 +348,7 @@ def run_gpu(args):
         "e2e": {"value": world * args.steps / e2e_elapsed, "unit": "steps/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "spmv_gbs": achieved,
+        "fp64_rel_err_vs_1e-12": {"u": eu64, "p": ep64},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
                      "kernel": "k_spmv<double> (node panels)", "launch_ms": spmv_ms,

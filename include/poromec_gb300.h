@@ -57,8 +57,8 @@ typedef struct {
 
 /* Precision modes (pm_set_precision). */
 #define PM_FP64 0          /* plain FP64: values, vectors and arithmetic */
-#define PM_FP32_REFINE 1   /* FP32 matrix values + FP32-valued inner Krylov
-                              solve inside an FP64 iterative-refinement loop */
+#define PM_FP32_REFINE 1   /* FP32 matrix values and FP32 SpMV in the inner PCG
+                              of an FP64 iterative-refinement loop */
 
 /* Mesh set-up: the 'mesh' macro (Main.f:481-870): equation numbering
  * numeqpmec2 (Numeq.f:86-151), CSRD structure datastruct_pm/csrstruct_pm
@@ -94,6 +94,9 @@ int pm_get_state(pm_handle h, double* u, double* u0, double* dp);
  * (initial_stress, Pform.f:679), added to b0 every step (Main.f:931-933). */
 int pm_set_initial_stress(pm_handle h, const double* tx0);
 int pm_set_precision(pm_handle h, int mode);
+/* PM_FP32_REFINE: relative tolerance of each inner FP32-operator PCG sweep
+ * (default 1e-5). */
+int pm_set_refine(pm_handle h, double inner_tol);
 
 int pm_get_sizes(pm_handle h, int* neq, int64_t* nad, int* numcolors,
                  int64_t* nnz_panel);

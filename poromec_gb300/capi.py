@@ -69,6 +69,7 @@ def load(path=None):
     lib.pm_get_state.argtypes = [c_p] * 4
     lib.pm_set_initial_stress.argtypes = [c_p, c_p]
     lib.pm_set_precision.argtypes = [c_p, c_i]
+    lib.pm_set_refine.argtypes = [c_p, c_d]
     lib.pm_get_sizes.argtypes = [c_p] * 5
     lib.pm_get_id.argtypes = [c_p, c_p]
     lib.pm_get_csrd.argtypes = [c_p] * 5
@@ -173,6 +174,9 @@ class Mesh:
 
     def set_precision(self, mode):
         self._check(self.lib.pm_set_precision(self.h, int(mode)), "pm_set_precision")
+
+    def set_refine(self, inner_tol=1e-5):
+        self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
 
     def get_id(self):
         idr = np.zeros((self.nnode, 4), np.int32)

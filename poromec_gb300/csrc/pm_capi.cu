@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -182,9 +183,9 @@ int assemble_K(Handle* h, bool fp32) {
     if (!h->P.val32) {
       PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
       h->pcg_graph_val = h->minres_graph_val = nullptr;
-      if (h->pcg32_graph) {
-        cudaGraphExecDestroy(h->pcg32_graph);
-        h->pcg32_graph = nullptr;
+      if (h->pcgm_graph) {
+        cudaGraphExecDestroy(h->pcgm_graph);
+        h->pcgm_graph = nullptr;
       }
     }
     PM_CUDA(cudaMemsetAsync(h->P.val32, 0, sizeof(float) * (size_t)h->P.nnz, h->stream));
@@ -373,35 +374,42 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   return PM_OK;
 }
 
-// FP64 iterative refinement around an FP32 PCG:
-// x = 0; repeat r = b - A64 x (FP64 panels, FP64 arithmetic), solve
-// A32 dx = r with PCG on FP32 values and FP32 vectors to a loose relative
-// tolerance, x += dx; stop when ||r||_|M| <= tol ||b||_|M|.  Residuals, the
-// norms and the diagonal preconditioner stay FP64.
-int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, int maxit,
-           pm_step_info* info) {
+// FP32 values + FP64 iterative refinement (PM_FP32_REFINE):
+//   x = 0, r = b
+//   repeat: if ||r||_|M| <= tol ||b||_|M|: done
+//           solve A32 dx = r by PCG (Iters.f:299-595 recurrences) whose
+//             products use the FP32 panel values and FP32 copies of the
+//             direction, everything else (vectors, dots, scalars) FP64,
+//             to a relative tolerance inner_tol
+//           x += dx;  r = b - A64 x  (FP64 panels, FP64 arithmetic)
+// ||.||_|M| = sqrt(sum |m_i| r_i^2) is a norm also on this indefinite
+// system.  An inner solve that stalls at the FP32 operator's rounding floor
+// stops at its iteration cap and hands its progress to the next sweep.
+int solve_mixed(Handle* h, int solver, const double* d_b, double* d_x, double tol, int maxit,
+                pm_step_info* info) {
   if (solver != 1) {
-    h->err = "FP32 refinement is implemented for PCG (solver 1)";
+    h->err = "the FP32 + FP64-refinement mode is implemented for PCG (solver 1)";
     return PM_E_ARG;
   }
   const int n = h->neq;
   const pm::PanelView P = h->P.view();
+  pm::KrylovVecs& V = h->D.kv;
+  pm::KrylovVecs32& V32 = h->D.kv32;
   double* r = h->D.rr;
-  pm::KrylovVecs32& V = h->D.kv32;
-  PM_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, h->stream));
-  PM_CUDA(cudaMemcpyAsync(r, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
-  if (!h->pcg32_graph) {
-    PM_TRY(capture(h, &h->pcg32_graph, [&]() {
-      return pm::pcg32_iteration(P, h->P.val32, n, V, h->D.ks, h->D.partial, h->D.counter,
-                                 h->stream);
+  if (!h->pcgm_graph) {
+    PM_TRY(capture(h, &h->pcgm_graph, [&]() {
+      return pm::pcgm_iteration(P, h->P.val32, n, h->D.m, V, V32, h->D.ks, h->D.partial,
+                                h->D.counter, h->stream);
     }));
   }
-  double bnorm = -1.0;
-  int total = 0, sweep = 0;
   cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
   PM_CUDA(cudaEventRecord(e0, h->stream));
-  for (sweep = 0; sweep < 60; ++sweep) {
-    // ||r||_|M| = sqrt(sum |m_i| r_i^2), a norm also on the indefinite system
+  PM_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, h->stream));
+  PM_CUDA(cudaMemcpyAsync(r, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  double bnorm = -1.0;
+  int total = 0, sweep = 0, cap = maxit;
+  const int kMaxSweeps = 30;
+  for (sweep = 0; sweep < kMaxSweeps; ++sweep) {
     double rn2 = 0.0;
     h->launches += 1;
     PM_CUDA(pm::wnorm2(n, r, h->D.m, h->D.norms, h->D.partial, h->D.counter, h->stream));
@@ -411,33 +419,40 @@ int refine(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     const double rn = std::sqrt(rn2);
     if (bnorm < 0) bnorm = rn;
     if (rn <= tol * bnorm || rn == 0.0) break;
-    // inner tolerance relative to the current residual, never tighter than
-    // needed for the outer target
-    const double itol = std::max(h->inner_tol, 0.5 * tol * bnorm / rn);
+    const double itol = std::max(h->inner_tol, 0.3 * tol * bnorm / rn);
     pm::KrylovScalars ks{};
     h->launches += 1;
-    PM_CUDA(pm::pcg32_init(n, r, h->D.m, V, h->D.ks, itol, maxit, h->D.partial, h->D.counter,
-                           h->stream));
+    PM_CUDA(pm::pcgm_init(n, r, h->D.m, V, V32, h->D.ks, itol, std::min(cap, maxit),
+                          h->D.partial, h->D.counter, h->stream));
     for (;;) {
-      PM_CUDA(cudaGraphLaunch(h->pcg32_graph, h->stream));
+      PM_CUDA(cudaGraphLaunch(h->pcgm_graph, h->stream));
       h->launches += 3 * kGraphIters;
       PM_TRY(read_scalars(h, &ks));
       if (ks.conv_flag) break;
     }
+    if (h->debug)
+      fprintf(stderr, "refine sweep %d: |r|_|M| %.3e / %.3e, inner tol %.1e, its %d, flag %d\n",
+              sweep, rn, bnorm, itol, ks.iter, ks.conv_flag);
     if (ks.conv_flag == 3) {
-      h->err = "refinement: inner PCG breakdown";
+      h->err = "refinement: inner PCG breakdown (non-finite recurrence)";
       return PM_E_NOCONV;
     }
     total += ks.iter;
+    if (sweep == 0) cap = std::max(200, 3 * ks.iter);
+    if (total > maxit) {
+      h->err = "refinement: no convergence after " + std::to_string(total) + " inner iterations";
+      if (info) info->iters = total;
+      return PM_E_NOCONV;
+    }
     // x += dx;  r = b - A64 x
     h->launches += 3;
-    PM_CUDA(pm::add_f32(n, d_x, V.x, h->stream));
+    PM_CUDA(pm::axpy_into(n, d_x, V.x, 1.0, h->stream));
     PM_CUDA(pm::spmv(P, h->P.val, nullptr, d_x, h->D.by, 0, nullptr, nullptr, nullptr,
                      h->stream));
     PM_CUDA(pm::vsub(n, r, d_b, h->D.by, h->stream));
   }
-  if (sweep == 60) {
-    h->err = "refinement: no convergence after 60 sweeps";
+  if (sweep == kMaxSweeps) {
+    h->err = "refinement: no convergence after " + std::to_string(kMaxSweeps) + " sweeps";
     return PM_E_NOCONV;
   }
   PM_CUDA(cudaEventRecord(e1, h->stream));
@@ -465,16 +480,16 @@ int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x
     if (!h->assembled32) {
       if (!h->P.val32) {
         PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
-        if (h->pcg32_graph) {
-          cudaGraphExecDestroy(h->pcg32_graph);
-          h->pcg32_graph = nullptr;
+        if (h->pcgm_graph) {
+          cudaGraphExecDestroy(h->pcgm_graph);
+          h->pcgm_graph = nullptr;
         }
       }
       h->launches += 1;
       PM_CUDA(pm::to_f32(h->P.nnz, h->P.val, h->P.val32, h->stream));
       h->assembled32 = true;
     }
-    return refine(h, solver, d_b, d_x, tol, maxit, info);
+    return solve_mixed(h, solver, d_b, d_x, tol, maxit, info);
   }
   return krylov(h, solver, d_b, d_x, tol, maxit, nullptr, info);
 }
@@ -510,7 +525,7 @@ int alloc_state(Handle* h) {
   PM_CUDA(cudaMalloc(&D.ks, sizeof(pm::KrylovScalars)));
   PM_CUDA(cudaMemset(D.ks, 0, sizeof(pm::KrylovScalars)));
   pm::KrylovVecs32& V32 = D.kv32;
-  for (float** p : {&V32.x, &V32.r, &V32.z, &V32.p, &V32.q, &V32.m}) {
+  for (float** p : {&V32.p, &V32.q}) {
     if (cudaMalloc((void**)p, sizeof(float) * std::max<size_t>(n, 1)) != cudaSuccess) {
       h->err = "cudaMalloc failed";
       return PM_E_NOMEM;
@@ -534,14 +549,13 @@ void free_all(Handle* h) {
                   D.ad, D.m, D.bx, D.by, D.rr, D.dx, D.xs, D.kv.x, D.kv.r, D.kv.z, D.kv.p, D.kv.q,
                   D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
-                  P.val32, P.node_val_off, P.node_W};
+                  P.val32, P.node_val_off, P.node_W, P.order};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (void* p : {(void*)D.kv32.x, (void*)D.kv32.r, (void*)D.kv32.z, (void*)D.kv32.p,
-                  (void*)D.kv32.q, (void*)D.kv32.m})
+  for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q})
     if (p) cudaFree(p);
   if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
-  if (h->pcg32_graph) cudaGraphExecDestroy(h->pcg32_graph);
+  if (h->pcgm_graph) cudaGraphExecDestroy(h->pcgm_graph);
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
@@ -651,6 +665,7 @@ int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
   if ((st = pm::build_structure(h, ix, id, fnno, x, num)) != PM_OK) return fail(st);
   if ((st = alloc_state(h)) != PM_OK) return fail(st);
   if ((st = upload_materials(h)) != PM_OK) return fail(st);
+  h->debug = getenv("PM_DEBUG") != nullptr;
   *out = reinterpret_cast<pm_handle>(h);
   return PM_OK;
 }
@@ -744,6 +759,13 @@ int pm_set_precision(pm_handle hh, int mode) {
   Handle* h = reinterpret_cast<Handle*>(hh);
   if (!h || (mode != PM_FP64 && mode != PM_FP32_REFINE)) return PM_E_ARG;
   h->precision = mode;
+  return PM_OK;
+}
+
+int pm_set_refine(pm_handle hh, double inner_tol) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !(inner_tol > 0.0 && inner_tol < 1.0)) return PM_E_ARG;
+  h->inner_tol = inner_tol;
   return PM_OK;
 }
 

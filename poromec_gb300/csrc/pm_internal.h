@@ -36,6 +36,7 @@ struct Panels {
   int nact = 0;           // nodes with at least one free dof
   int64_t nnz = 0;        // sum d_I W_I
   int64_t ncols = 0;      // sum W_I
+  int32_t* order = nullptr;  // active nodes sorted by (d, W) for the SpMV
   int32_t* eq0 = nullptr;
   int32_t* d = nullptr;
   int32_t* W = nullptr;
@@ -49,7 +50,7 @@ struct Panels {
   int64_t* node_val_off = nullptr;
   int32_t* node_W = nullptr;
   PanelView view() const {
-    return PanelView{nact, eq0, d, W, low, val_off, col_off, cols};
+    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols};
   }
 };
 
@@ -119,7 +120,8 @@ struct Handle {
   int64_t nad = 0;
   int numcolors = 0;
   int precision = PM_FP64;
-  double inner_tol = 1.0e-5;   // inner Krylov tolerance of the FP32 refinement
+  double inner_tol = 1.0e-5;   // inner tolerance of the FP32 refinement sweeps
+  bool debug = false;          // PM_DEBUG set: solver progress on stderr
   std::vector<int32_t> color_ptr;
   std::vector<int32_t> h_eq;       // (ndf, nnode)
   std::vector<int32_t> h_fnno;
@@ -143,7 +145,7 @@ struct Handle {
   Dev D;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
-  cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr, pcg32_graph = nullptr;
+  cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr, pcgm_graph = nullptr;
   const void* pcg_graph_val = nullptr;   // values pointer baked into the graph
   const void* minres_graph_val = nullptr;
   const double* pcg_graph_m = nullptr;

@@ -13,6 +13,7 @@ constexpr int kRedBlocks = 1216;
 // Read-only view of the node panels passed by value to kernels.
 struct PanelView {
   int nact;
+  const int32_t* order;    // SpMV visiting order: active nodes sorted by (d, W)
   const int32_t* eq0;      // first equation (0-based) per active node
   const int32_t* d;        // free dofs per active node
   const int32_t* W;        // panel width
@@ -39,21 +40,19 @@ struct KrylovVecs {
   double *v, *v0, *w0, *w00, *z0;   // MINRES (also uses x, z, p, q)
 };
 
-// FP32 vectors of the refinement's inner PCG.
+// FP32 copies used by the mixed-precision PCG: the search direction and
+// its product with the FP32 matrix.
 struct KrylovVecs32 {
-  float *x, *r, *z, *p, *q, *m;
+  float *p, *q;
 };
 
 int vec_grid(int n);
-cudaError_t spmv32(const PanelView& P, const float* val32, const float* x, float* y, int mode,
-                   KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s);
-cudaError_t pcg32_init(int n, const double* b, const double* m, KrylovVecs32& V,
-                       KrylovScalars* ks, double tol, int maxit, double* partial,
-                       unsigned* counter, cudaStream_t s);
-cudaError_t pcg32_iteration(const PanelView& P, const float* val32, int n, KrylovVecs32& V,
-                            KrylovScalars* ks, double* partial, unsigned* counter,
-                            cudaStream_t s);
-cudaError_t add_f32(int n, double* y, const float* x, cudaStream_t s);
+cudaError_t pcgm_init(int n, const double* b, const double* m, KrylovVecs& V,
+                      KrylovVecs32& V32, KrylovScalars* ks, double tol, int maxit,
+                      double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t pcgm_iteration(const PanelView& P, const float* val32, int n, const double* m,
+                           KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                           double* partial, unsigned* counter, cudaStream_t s);
 cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
                  const double* x, double* y, int mode, KrylovScalars* ks,
                  double* partial, unsigned* counter, cudaStream_t s);

@@ -239,6 +239,15 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
   P.nnz = vo;
   P.ncols = co;
   int st;
+  // SpMV visiting order: by free dofs, then panel width (descending), then
+  // equation order, so the nodes sharing a warp run identical loops
+  std::vector<int32_t> order(nact);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
+    return h->h_W[a] > h->h_W[b];
+  });
+  if ((st = upload(h, &P.order, order.data(), nact))) return st;
   if ((st = upload(h, &P.eq0, h->h_eq0.data(), nact))) return st;
   if ((st = upload(h, &P.d, h->h_d.data(), nact))) return st;
   if ((st = upload(h, &P.W, h->h_W.data(), nact))) return st;

@@ -95,7 +95,12 @@ __device__ __forceinline__ bool krylov_skip(KrylovScalars* ks, bool first) {
 //
 // MODE 0: y = A x.   MODE 1: PCG, also alpha = d / (y . x).
 // MODE 2: MINRES, also alpha = |x . y| / beta^2.   MODE 3: y = A x and
-// ks->xkx = x . y (energy norm of the solver log).
+// ks->xkx = x . y (energy norm of the solver log).   MODE 4: mixed PCG,
+// FP32 operator, alpha = d / (y . xd) with the FP64 direction xd.
+//
+// Nodes are visited in P.order, sorted by (d, W): the 4 sub-warps of a warp
+// then run the same loop, so FP64 instructions issue with full lane masks
+// (on GB300 a partial-mask FP64 instruction costs the full pipe time).
 constexpr int kSub = 8;
 
 template <typename T>
@@ -106,20 +111,22 @@ __device__ __forceinline__ T shfl(T v, int m) {
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256)
     k_spmv(PanelView P, const T* __restrict__ val, const T* __restrict__ x,
-           T* __restrict__ y, KrylovScalars* ks, double* partial, unsigned* counter) {
-  if (MODE == 1 || MODE == 2)
+           T* __restrict__ y, KrylovScalars* ks, double* partial, unsigned* counter,
+           const double* __restrict__ xd = nullptr) {
+  if (MODE == 1 || MODE == 2 || MODE == 4)
     if (krylov_skip(ks, true)) return;
   const int lane = threadIdx.x & 31;
   const int t = lane & (kSub - 1);
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
   constexpr int kNodesPerWarp = 32 / kSub;
-  T dsum = T(0);
+  double dsum = 0.0;
   for (int base = warp * kNodesPerWarp; base < P.nact; base += nwarp * kNodesPerWarp) {
-    const int node = base + (lane >> 3);
+    const int slot = base + (lane >> 3);
+    const int node = slot < P.nact ? P.order[slot] : 0;
     int e0 = 0, d = 0, W = 0;
     T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-    if (node < P.nact) {
+    if (slot < P.nact) {
       e0 = P.eq0[node];
       d = P.d[node];
       W = P.W[node];
@@ -159,13 +166,14 @@ __global__ void __launch_bounds__(256)
     const int r = (h4 ? 2 : 0) + (h2 ? 1 : 0);
     if ((t & 1) == 0 && r < d) {
       y[e0 + r] = k;
-      if (MODE != 0) dsum += k * x[e0 + r];
+      if (MODE == 4) dsum += double(k) * xd[e0 + r];
+      else if (MODE != 0) dsum += double(k * x[e0 + r]);
     }
   }
   if (MODE != 0) {
-    double in[1] = {double(dsum)}, tot[1];
+    double in[1] = {dsum}, tot[1];
     if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
-      if (MODE == 1) {
+      if (MODE == 1 || MODE == 4) {
         ks->pq = tot[0];
         ks->alpha = ks->d / tot[0];
       } else if (MODE == 2) {
@@ -245,24 +253,23 @@ __global__ void __launch_bounds__(256)
     p[i] = z[i] + beta * p[i];
 }
 
-// ---- FP32 inner PCG of the refinement --------------------------------------
-// The same recurrences on FP32 vectors and the FP32 panel values; dot
-// products accumulate per thread in FP32 and across threads in FP64.
+// ---- mixed-precision PCG (inner solve of the FP64 refinement) ----------------
+// The recurrences of pcg on FP64 vectors and scalars; only the product
+// q = A p uses the FP32 panel values and FP32 copies of p and q.
 __global__ void __launch_bounds__(256)
-    k_pcg32_init(int n, const double* __restrict__ b, const double* __restrict__ m,
-                 float* __restrict__ m32, float* __restrict__ r, float* __restrict__ z,
-                 float* __restrict__ p, float* __restrict__ x, KrylovScalars* ks, double tol,
-                 int maxit, double* partial, unsigned* counter) {
+    k_pcgm_init(int n, const double* __restrict__ b, const double* __restrict__ m,
+                double* __restrict__ r, double* __restrict__ z, double* __restrict__ p,
+                float* __restrict__ p32, double* __restrict__ x, KrylovScalars* ks, double tol,
+                int maxit, double* partial, unsigned* counter) {
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float mi = float(m[i]);
-    const float bi = float(b[i]), zi = bi * mi;
-    m32[i] = mi;
-    x[i] = 0.f;
+    const double bi = b[i], zi = bi * m[i];
+    x[i] = 0.0;
     r[i] = bi;
     z[i] = zi;
     p[i] = zi;
-    acc += double(bi * zi);
+    p32[i] = float(zi);
+    acc += bi * zi;
   }
   double in[1] = {acc}, tot[1];
   if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
@@ -277,22 +284,22 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void __launch_bounds__(256)
-    k_pcg32_update(int n, float* __restrict__ x, const float* __restrict__ p,
-                   float* __restrict__ r, const float* __restrict__ q,
-                   const float* __restrict__ m, float* __restrict__ z, KrylovScalars* ks,
-                   double* partial, unsigned* counter) {
+    k_pcgm_update(int n, double* __restrict__ x, const double* __restrict__ p,
+                  double* __restrict__ r, const float* __restrict__ q32,
+                  const double* __restrict__ m, double* __restrict__ z, KrylovScalars* ks,
+                  double* partial, unsigned* counter) {
   if (krylov_skip(ks, false)) return;
-  const float alpha = float(ks->alpha);
-  float acc = 0.f;
+  const double alpha = ks->alpha;
+  double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] = x[i] + alpha * p[i];
-    const float ri = r[i] - alpha * q[i];
+    const double ri = r[i] - alpha * double(q32[i]);
     r[i] = ri;
-    const float zi = ri * m[i];
+    const double zi = ri * m[i];
     z[i] = zi;
     acc += ri * zi;
   }
-  double in[1] = {double(acc)}, tot[1];
+  double in[1] = {acc}, tot[1];
   if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
     const double di = tot[0];
     ks->beta = di / ks->d;
@@ -305,17 +312,15 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void __launch_bounds__(256)
-    k_pcg32_dir(int n, const float* __restrict__ z, float* __restrict__ p, KrylovScalars* ks) {
+    k_pcgm_dir(int n, const double* __restrict__ z, double* __restrict__ p,
+               float* __restrict__ p32, KrylovScalars* ks) {
   if (krylov_skip(ks, false)) return;
-  const float beta = float(ks->beta);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
-}
-
-// x64 += double(x32)
-__global__ void k_add_f32(int n, double* __restrict__ y, const float* __restrict__ x) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    y[i] += double(x[i]);
+  const double beta = ks->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double pi = z[i] + beta * p[i];
+    p[i] = pi;
+    p32[i] = float(pi);
+  }
 }
 
 // ---- MINRES ----------------------------------------------------------------
@@ -588,35 +593,22 @@ cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
   return cudaGetLastError();
 }
 
-cudaError_t spmv32(const PanelView& P, const float* val32, const float* x, float* y, int mode,
-                   KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s) {
-  const int grid = kRedBlocks;
-  if (mode == 0) k_spmv<float, 0><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter);
-  else k_spmv<float, 1><<<grid, 256, 0, s>>>(P, val32, x, y, ks, partial, counter);
+cudaError_t pcgm_init(int n, const double* b, const double* m, KrylovVecs& V,
+                      KrylovVecs32& V32, KrylovScalars* ks, double tol, int maxit,
+                      double* partial, unsigned* counter, cudaStream_t s) {
+  k_pcgm_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.r, V.z, V.p, V32.p, V.x, ks, tol, maxit,
+                                           partial, counter);
   return cudaGetLastError();
 }
 
-cudaError_t pcg32_init(int n, const double* b, const double* m, KrylovVecs32& V,
-                       KrylovScalars* ks, double tol, int maxit, double* partial,
-                       unsigned* counter, cudaStream_t s) {
-  k_pcg32_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.m, V.r, V.z, V.p, V.x, ks, tol, maxit,
-                                            partial, counter);
-  return cudaGetLastError();
-}
-
-cudaError_t pcg32_iteration(const PanelView& P, const float* val32, int n, KrylovVecs32& V,
-                            KrylovScalars* ks, double* partial, unsigned* counter,
-                            cudaStream_t s) {
-  cudaError_t e = spmv32(P, val32, V.p, V.q, 1, ks, partial, counter, s);
-  if (e != cudaSuccess) return e;
-  k_pcg32_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, V.m, V.z, ks, partial,
-                                              counter);
-  k_pcg32_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, ks);
-  return cudaGetLastError();
-}
-
-cudaError_t add_f32(int n, double* y, const float* x, cudaStream_t s) {
-  k_add_f32<<<vec_grid(n), 256, 0, s>>>(n, y, x);
+cudaError_t pcgm_iteration(const PanelView& P, const float* val32, int n, const double* m,
+                           KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                           double* partial, unsigned* counter, cudaStream_t s) {
+  k_spmv<float, 4><<<kRedBlocks, 256, 0, s>>>(P, val32, V32.p, V32.q, ks, partial, counter,
+                                               V.p);
+  k_pcgm_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V32.q, m, V.z, ks, partial,
+                                             counter);
+  k_pcgm_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, V32.p, ks);
   return cudaGetLastError();
 }
 
