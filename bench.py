@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--solvtol", type=float, default=1e-8)
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="one step of the same workload only (for the ncu launch list)")
     return ap.parse_args()
 
 
@@ -230,6 +232,12 @@ def run_gpu(args):
     m = pg.from_problem(pb)
     step_kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=args.solvtol,
                    maxit=200000, reassemble=True)
+    if args.profile:
+        info = m.step(**step_kw)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_step": True, "pcg_iterations": info.iters,
+                          "kernels": int(m.timers()[7])}), flush=True)
+        return
     for _ in range(args.warmup):
         m.step(**step_kw)
     snap = m.get_state()
@@ -284,7 +292,10 @@ def run_gpu(args):
         ep = float(np.abs(a[:, 3] - u_ref[:, 3]).max() / np.abs(u_ref[:, 3]).max())
         return eu, ep
 
-    # FP32 values + FP64 refinement from the same state
+    # FP32 values + FP64 refinement from the same state, bounded to twice the
+    # FP64 iteration count per step: on this indefinite system the FP32
+    # operator's rounding, amplified by the conditioning, can stall the
+    # refinement, and the bench reports that instead of waiting.
     mixed = None
     if not args.no_mixed:
         restore()
@@ -293,19 +304,25 @@ def run_gpu(args):
         barrier()
         t0 = time.perf_counter()
         mi = []
-        for _ in range(args.steps):
-            info = m.step(**step_kw)
-            mi.append((info.iters, info.refine))
-        barrier()
-        t_mixed = time.perf_counter() - t0
-        u32, _, _ = m.get_state()
+        try:
+            for _ in range(args.steps):
+                info = m.step(**dict(step_kw, maxit=2 * max(iters)))
+                mi.append((info.iters, info.refine))
+            barrier()
+            t_mixed = time.perf_counter() - t0
+            u32, _, _ = m.get_state()
+            eu, ep = rel_err(u32)
+            mixed = {"value": world * args.steps / t_mixed, "unit": "steps/s",
+                     "speedup_vs_fp64": (args.steps / t_mixed) / (args.steps / elapsed),
+                     "rel_err_u_vs_fp64_1e-12": eu, "rel_err_p_vs_fp64_1e-12": ep,
+                     "inner_iterations_per_step": [a for a, _ in mi],
+                     "refine_sweeps_per_step": [b for _, b in mi]}
+        except pg.PMError as ex:
+            torch.cuda.synchronize()
+            mixed = {"value": None, "unit": "steps/s", "status": "no convergence",
+                     "detail": str(ex), "steps_completed": len(mi),
+                     "iteration_budget_per_step": 2 * max(iters)}
         m.set_precision(pg.capi.PM_FP64)
-        eu, ep = rel_err(u32)
-        mixed = {"value": world * args.steps / t_mixed, "unit": "steps/s",
-                 "speedup_vs_fp64": (args.steps / t_mixed) / (args.steps / elapsed),
-                 "rel_err_u_vs_fp64_1e-12": eu, "rel_err_p_vs_fp64_1e-12": ep,
-                 "inner_iterations_per_step": [a for a, _ in mi],
-                 "refine_sweeps_per_step": [b for _, b in mi]}
     eu64, ep64 = rel_err(u64)
 
     # SpMV roofline: the dominant kernel timed alone with CUDA events on the
