@@ -42,7 +42,8 @@ typedef enum {
   PM_E_ELTYPE = 6,     /* element type other than 15 (tetra10) / 17 (hexa20) */
   PM_E_CUDA = 7,       /* CUDA runtime error (message in pm_last_error) */
   PM_E_NOMEM = 8,      /* device allocation failed */
-  PM_E_STATE = 9       /* call out of order (e.g. solve before assembly) */
+  PM_E_STATE = 9,      /* call out of order (e.g. solve before assembly) */
+  PM_E_TOO_LARGE = 10  /* larger than the fixed scratch of pm_pcg_csrd_noalloc */
 } pm_status;
 
 typedef struct {
@@ -145,6 +146,25 @@ int pm_solve_dev(pm_handle h, int solver, int precond, const double* d_b,
 int pm_matvec_csrd_dev(int neq, const int64_t* d_ia, const int32_t* d_ja,
                        const double* d_ad, const double* d_al,
                        const double* d_x, double* d_y, void* stream);
+
+/* Solve without device allocation.  No counterpart in the reference: it
+ * serves callers that must not allocate device memory while they solve (a
+ * driver whose memory belongs to its own arena, a framework that owns the
+ * device pool, a latency-bound step).  It runs the PCG of pm_solve (solver 1,
+ * precond 2: m = 1/ad) on the reference CSRD arrays the caller already holds
+ * on the device (d_ia int64 1-based, d_ja int32 1-based, d_ad, d_al), with
+ * right-hand side d_b and solution d_x (set to 0 first), length neq.  All
+ * scratch comes from one array compiled into the library: each GPU that
+ * loads the library holds about 10.5 MB for it until the process exits, and
+ * neq above PM_NOALLOC_MAX_NEQ returns PM_E_TOO_LARGE.  The first call on a
+ * device looks up that array's device address, so make it before any stream
+ * capture.  Calls share the array and it keeps the last call's contents:
+ * two calls that run at the same time on one GPU (two streams, two host
+ * threads) race, so serialise them.  stream may be NULL (legacy stream). */
+#define PM_NOALLOC_MAX_NEQ 262144
+int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* d_ja,
+                        const double* d_ad, const double* d_al, const double* d_b,
+                        double* d_x, double tol, int maxit, int* iters, void* stream);
 
 /* Timing of the last pm_step phases in milliseconds (CUDA events):
  * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,

@@ -617,6 +617,7 @@ const char* pm_status_string(int s) {
     case PM_E_CUDA: return "CUDA error";
     case PM_E_NOMEM: return "device allocation failed";
     case PM_E_STATE: return "call out of order";
+    case PM_E_TOO_LARGE: return "problem larger than the fixed scratch of pm_pcg_csrd_noalloc";
     default: return "unknown status";
   }
 }

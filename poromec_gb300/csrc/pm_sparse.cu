@@ -14,6 +14,9 @@
 // convergence without changing the result.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
+#include "../../include/poromec_gb300.h"
 #include "pm_krylov.h"
 
 namespace pm {
@@ -718,4 +721,152 @@ cudaError_t to_f32(int64_t n, const double* a, float* b, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+
+// ---- solve without device allocation ---------------------------------------
+// pm_pcg_csrd_noalloc: the diagonal-preconditioned PCG of pm_solve, on the
+// reference CSRD arrays the caller already holds on the device, taking every
+// scratch vector and reduction buffer from one fixed array compiled into the
+// library.  It exists for callers that may not allocate device memory while
+// they solve: a Fortran driver whose memory is owned by its own arena (the
+// reference's Malloc.f style), code running inside a framework that has
+// reserved the device memory pool, or a step that must not pay the latency
+// of cudaMalloc.  The array is a file-scope __device__ symbol: every GPU that
+// loads the library holds PM_NOALLOC_MAX_NEQ * 5 doubles plus the reduction
+// buffers (about 10.5 MB) until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxNeq = PM_NOALLOC_MAX_NEQ;
+constexpr size_t kNoAllocVec = (size_t)kNoAllocMaxNeq;
+// layout (doubles): m, r, z, p, q (kNoAllocVec each), partials (2 * kRedBlocks),
+// solver scalars (KrylovScalars), counter + zero-diagonal flag
+constexpr size_t kNoAllocPartial = 5 * kNoAllocVec;
+constexpr size_t kNoAllocScalars = kNoAllocPartial + 2 * (size_t)kRedBlocks;
+constexpr size_t kNoAllocFlags = kNoAllocScalars + 64;
+constexpr size_t kNoAllocDoubles = kNoAllocFlags + 8;
+static_assert(sizeof(KrylovScalars) <= 64 * sizeof(double), "scalars region too small");
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// (cudaGetSymbolAddress with that device current).
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+// alpha = d / (p, q) for the CSRD product q = A p
+__global__ void __launch_bounds__(256)
+    k_noalloc_alpha(int n, const double* __restrict__ p, const double* __restrict__ q,
+                    KrylovScalars* ks, double* partial, unsigned* counter) {
+  if (krylov_skip(ks, true)) return;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    acc += p[i] * q[i];
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    ks->pq = tot[0];
+    ks->alpha = ks->d / tot[0];
+  }
+}
+
+// q = A p on the CSRD layout, skipped once the solve has converged
+__global__ void __launch_bounds__(256)
+    k_noalloc_csrd(int neq, const int64_t* __restrict__ ia, const int32_t* __restrict__ ja,
+                   const double* __restrict__ ad, const double* __restrict__ al,
+                   const double* __restrict__ x, double* __restrict__ y,
+                   const KrylovScalars* ks) {
+  if (ks->done || ks->conv_flag) return;
+  const int lane = threadIdx.x & 31;
+  const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < neq; i += nw) {
+    const double xi = x[i];
+    double t = 0.0;
+    for (int64_t k = ia[i] - 1 + lane; k < ia[i + 1] - 1; k += 32) {
+      const int j = ja[k] - 1;
+      const double s = al[k];
+      t += s * x[j];
+      atomicAdd(&y[j], s * xi);
+    }
+    t = warp_sum(t);
+    if (lane == 0) atomicAdd(&y[i], t + ad[i] * xi);
+  }
+}
+
+__global__ void k_noalloc_zero(int n, double* __restrict__ y, const KrylovScalars* ks) {
+  if (ks->done || ks->conv_flag) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    y[i] = 0.0;
+}
+
+}  // namespace
+
+}  // namespace pm
+
+extern "C" int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* d_ja,
+                                   const double* d_ad, const double* d_al, const double* d_b,
+                                   double* d_x, double tol, int maxit, int* iters,
+                                   void* stream) {
+  using namespace pm;
+  if (neq > kNoAllocMaxNeq) return PM_E_TOO_LARGE;
+  if (neq <= 0 || !d_ia || !d_ja || !d_ad || !d_al || !d_b || !d_x || maxit < 1 || !(tol >= 0.0))
+    return PM_E_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
+    return PM_E_CUDA;
+  double* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return PM_E_CUDA;
+      g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  double* m = base;
+  KrylovVecs V{};
+  V.x = d_x;
+  V.r = base + kNoAllocVec;
+  V.z = base + 2 * kNoAllocVec;
+  V.p = base + 3 * kNoAllocVec;
+  V.q = base + 4 * kNoAllocVec;
+  double* partial = base + kNoAllocPartial;
+  KrylovScalars* ks = reinterpret_cast<KrylovScalars*>(base + kNoAllocScalars);
+  unsigned* counter = reinterpret_cast<unsigned*>(base + kNoAllocFlags);
+  int* zero_diag = reinterpret_cast<int*>(base + kNoAllocFlags + 1);
+  // the array keeps the previous call's contents: the counter and the flag
+  // must start at zero; every vector is written before it is read
+  if (cudaMemsetAsync(base + kNoAllocFlags, 0, 2 * sizeof(double), s) != cudaSuccess)
+    return PM_E_CUDA;
+  const int g = vec_grid(neq);
+  k_precond<<<g, 256, 0, s>>>(neq, d_ad, m, 0, zero_diag);
+  k_pcg_init<<<g, 256, 0, s>>>(neq, d_b, m, V.r, V.z, V.p, V.x, ks, tol, maxit, partial,
+                                counter);
+  int zd = 0;
+  if (cudaMemcpyAsync(&zd, zero_diag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return PM_E_CUDA;
+  if (zd) return PM_E_ZERO_DIAG;
+  int sgrid = (neq + 7) / 8;
+  if (sgrid > 8 * kRedBlocks) sgrid = 8 * kRedBlocks;
+  KrylovScalars h{};
+  for (;;) {
+    for (int k = 0; k < 16; ++k) {
+      k_noalloc_zero<<<g, 256, 0, s>>>(neq, V.q, ks);
+      k_noalloc_csrd<<<sgrid, 256, 0, s>>>(neq, d_ia, d_ja, d_ad, d_al, V.p, V.q, ks);
+      k_noalloc_alpha<<<g, 256, 0, s>>>(neq, V.p, V.q, ks, partial, counter);
+      k_pcg_update<<<g, 256, 0, s>>>(neq, V.x, V.p, V.r, V.q, m, V.z, ks, partial, counter);
+      k_pcg_dir<<<g, 256, 0, s>>>(neq, V.z, V.p, ks);
+    }
+    if (cudaGetLastError() != cudaSuccess) return PM_E_CUDA;
+    if (cudaMemcpyAsync(&h, ks, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return PM_E_CUDA;
+    if (h.conv_flag) break;
+  }
+  if (iters) *iters = h.iter;
+  return h.conv_flag == 1 ? PM_OK : PM_E_NOCONV;
+}
+
+namespace pm {
 }  // namespace pm
