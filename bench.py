@@ -1,7 +1,7 @@
 """Benchmark: implicit-Euler Biot steps/s of the heterogeneous hexa20 cube.
 
-Workload (the BASELINE metric's configuration that fits one GPU): structured
-56^3 hexa20 mesh of the unit cube, 731,025 nodes, 2,346,120 free equations
+Workload (the configuration the headline metric is quoted on; it fits one
+GPU): structured 56^3 hexa20 mesh of the unit cube, 731,025 nodes, 2,346,120 free equations
 (2.38 M dofs before boundary conditions), log-permeability Gaussian random
 field (mean ln 1e-14 m^2, sigma 1, correlation length 0.1 m), lognormal E
 (median 1 GPa, sigma_ln 0.3), nu = 0.25, base fixed, drained top, top
@@ -12,9 +12,14 @@ isw 4 element loop, K re-assembled from the elements (isw 2, as the
 reference does every step), residual, diagonal-PCG solve to 1e-8, residual
 check, state update.  `value` is steps/s with the state resident in HBM;
 `e2e` is the same step through the C ABI with the nodal state copied from
-and back to pinned host buffers every step.
+and back to pinned host buffers every step.  `fp32_refine` is the same
+timed steps with the matrix values held as FP32 + an int8 relative
+correction and the compensated FP32 SpMV inside the FP64 refinement loop (PM_FP32C_REFINE),
+with its error against the FP64 steps and against an FP64 solve at 1e-12.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+  python bench.py --spmv-only [--n 32] [--reps 20] [--precision fp64|fp32c]
+      (the SpMV alone on an assembled cube: the command the ncu summaries use)
 
 N > 1 runs N independent replicas (one per GPU; a single mesh does not
 shard without the halo exchange of the reference's MPI path).
@@ -48,6 +53,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one step of the same workload only (for the ncu launch list)")
+    ap.add_argument("--fp32-plain", action="store_true",
+                    help="also time the plain FP32-value refinement (PM_FP32_REFINE)")
+    ap.add_argument("--spmv-only", action="store_true",
+                    help="time the SpMV alone on the assembled cube of --n")
+    ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"])
     return ap.parse_args()
 
 
@@ -120,16 +131,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def spmv_bytes(nad, neq):
-    """Algorithmic bytes of one CSRD SpMV (FP64): each stored lower value and
-    its int32 column once, ad, x, y and the int32 row pointer once."""
-    return 12 * nad + 28 * neq
+def spmv_bytes(nad, neq, comp=False):
+    """Algorithmic bytes of one CSRD SpMV: each stored lower value and its
+    int32 column once, ad, x, y and the int32 row pointer once.  FP64:
+    12 nad + 28 neq.  Compensated (values FP32 + int8 = 5 B, x as an FP32
+    pair, y FP64): 9 nad + 25 neq."""
+    return (9 * nad + 25 * neq) if comp else (12 * nad + 28 * neq)
 
 
-def profile_traffic(nnz_panel):
+def profile_traffic(nnz_panel, name="spmv_panel_fp64_cube.md"):
     """DRAM bytes per SpMV launch from the committed ncu summary (bytes per
     panel nonzero measured on a smaller cube, scaled to this launch)."""
-    p = os.path.join(ROOT, "profiles", "spmv_panel_fp64_cube.md")
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -213,6 +226,46 @@ def run_reference(args):
 # --------------------------------------------------------------------------
 # GPU arm
 # --------------------------------------------------------------------------
+def time_spmv(m, torch, reps):
+    """Mean duration (ms) of pm_spmv_dev over reps launches, CUDA events on
+    the launching stream, after 5 warm-up launches.  The panel values
+    (>= 0.68 GB at n >= 32) exceed L2, so every launch streams them from HBM."""
+    x = torch.randn(m.neq, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    s = torch.cuda.Stream()  # a real stream handle (0 would select the library's own)
+    for _ in range(5):
+        m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_spmv_only(args):
+    import torch
+    import poromec_gb300 as pg
+    from poromec_gb300 import meshgen
+    pb = meshgen.cube_problem(args.n)
+    m = pg.from_problem(pb)
+    m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+    comp = args.precision == "fp32c"
+    shape = None
+    if comp:
+        m.set_precision(pg.capi.PM_FP32C_REFINE)
+        shape = m.tune_spmv()
+    ms = time_spmv(m, torch, args.reps)
+    B = spmv_bytes(m.nad, m.neq, comp)
+    print(json.dumps({"spmv_only": True, "n": args.n, "precision": args.precision,
+                      "shape": shape,
+                      "neq": m.neq, "nad": m.nad, "nnz_panel": m.nnz_panel, "launch_ms": ms,
+                      "algorithmic_bytes": B, "achieved_gbs": B / (ms * 1e-3) / 1e9}),
+          flush=True)
+
+
 def run_gpu(args):
     import torch
     rank, world, local = dist_env()
@@ -292,15 +345,14 @@ def run_gpu(args):
         ep = float(np.abs(a[:, 3] - u_ref[:, 3]).max() / np.abs(u_ref[:, 3]).max())
         return eu, ep
 
-    # FP32 values + FP64 refinement from the same state, bounded to twice the
-    # FP64 iteration count per step: on this indefinite system the FP32
-    # operator's rounding, amplified by the conditioning, can stall the
-    # refinement, and the bench reports that instead of waiting.
-    mixed = None
-    if not args.no_mixed:
+    def mixed_leg(mode, refine=None):
+        """The timed steps again from the same state in another precision
+        mode, bounded to twice the FP64 iteration count per step so that a
+        stalled refinement is reported instead of waited for."""
         restore()
-        m.set_precision(pg.capi.PM_FP32_REFINE)
-        m.set_refine(1e-5)
+        m.set_precision(mode)
+        if refine:
+            m.set_refine(refine)
         barrier()
         t0 = time.perf_counter()
         mi = []
@@ -310,37 +362,44 @@ def run_gpu(args):
                 mi.append((info.iters, info.refine))
             barrier()
             t_mixed = time.perf_counter() - t0
-            u32, _, _ = m.get_state()
-            eu, ep = rel_err(u32)
-            mixed = {"value": world * args.steps / t_mixed, "unit": "steps/s",
-                     "speedup_vs_fp64": (args.steps / t_mixed) / (args.steps / elapsed),
-                     "rel_err_u_vs_fp64_1e-12": eu, "rel_err_p_vs_fp64_1e-12": ep,
-                     "inner_iterations_per_step": [a for a, _ in mi],
-                     "refine_sweeps_per_step": [b for _, b in mi]}
+            um, _, _ = m.get_state()
+            eu, ep = rel_err(um)
+            du = float(np.abs(um[:, :3] - u64[:, :3]).max() / np.abs(u64[:, :3]).max())
+            dp_ = float(np.abs(um[:, 3] - u64[:, 3]).max() / np.abs(u64[:, 3]).max())
+            out = {"value": world * args.steps / t_mixed, "unit": "steps/s",
+                   "speedup_vs_fp64": elapsed / t_mixed,
+                   "rel_err_vs_fp64_same_tol": {"u": du, "p": dp_},
+                   "rel_err_vs_fp64_1e-12": {"u": eu, "p": ep},
+                   "pcg_iterations_per_step": [a for a, _ in mi],
+                   "refine_sweeps_per_step": [b for _, b in mi]}
         except pg.PMError as ex:
             torch.cuda.synchronize()
-            mixed = {"value": None, "unit": "steps/s", "status": "no convergence",
-                     "detail": str(ex), "steps_completed": len(mi),
-                     "iteration_budget_per_step": 2 * max(iters)}
-        m.set_precision(pg.capi.PM_FP64)
+            out = {"value": None, "unit": "steps/s", "status": "no convergence",
+                   "detail": str(ex), "steps_completed": len(mi),
+                   "iteration_budget_per_step": 2 * max(iters)}
+        return out
+
+    mixed = plain32 = None
+    if not args.no_mixed:
+        mixed = mixed_leg(pg.capi.PM_FP32C_REFINE)
+        # the compensated SpMV alone (x split into its FP32 pair included)
+        cms = time_spmv(m, torch, 50)
+        cB = spmv_bytes(m.nad, m.neq, comp=True)
+        ctr = profile_traffic(m.nnz_panel, "spmv_panel_fp32c_cube.md")
+        mixed["spmv"] = {"kernel": "k_spmv_cf<0> + k_split_pair", "launch_ms": cms,
+                         "shape": m.tune_spmv(),
+                         "algorithmic_bytes": cB, "achieved_gbs": cB / (cms * 1e-3) / 1e9,
+                         "traffic": ctr}
+        mixed["values"] = ("FP32 + int8 relative correction (5 B, 2^-32), compensated FP32 "
+                           "products and sums, FP64 vectors and dots")
+    if args.fp32_plain:
+        plain32 = mixed_leg(pg.capi.PM_FP32_REFINE, 1e-5)
+    m.set_precision(pg.capi.PM_FP64)
     eu64, ep64 = rel_err(u64)
 
     # SpMV roofline: the dominant kernel timed alone with CUDA events on the
     # stream it is launched on, 50 launches over the assembled matrix
-    x = torch.randn(m.neq, dtype=torch.float64, device="cuda")
-    y = torch.empty_like(x)
-    s = torch.cuda.Stream()  # a real stream handle (0 would select the library's own)
-    for _ in range(5):
-        m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    nl = 50
-    e0.record(s)
-    for _ in range(nl):
-        m.spmv_dev(x.data_ptr(), y.data_ptr(), s.cuda_stream)
-    e1.record(s)
-    torch.cuda.synchronize()
-    spmv_ms = e0.elapsed_time(e1) / nl
+    spmv_ms = time_spmv(m, torch, 50)
     B = spmv_bytes(m.nad, m.neq)
     achieved = B / (spmv_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
@@ -375,6 +434,8 @@ def run_gpu(args):
     }
     if mixed:
         out["fp32_refine"] = mixed
+    if plain32:
+        out["fp32_plain_refine"] = plain32
     if not args.no_cpu:
         t_step, parts, sample, threads = cpu_step_estimate(pb, int(np.mean(iters)))
         out["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads,
@@ -387,7 +448,9 @@ def run_gpu(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.spmv_only:
+        run_spmv_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -60,6 +60,11 @@ typedef struct {
 #define PM_FP64 0          /* plain FP64: values, vectors and arithmetic */
 #define PM_FP32_REFINE 1   /* FP32 matrix values and FP32 SpMV in the inner PCG
                               of an FP64 iterative-refinement loop */
+#define PM_FP32C_REFINE 2  /* matrix values as FP32 + an int8 relative correction
+                              (5 bytes, 2^-32 relative) and compensated FP32
+                              SpMV inside PCG / MINRES with FP64 vectors and
+                              dots, in an FP64 iterative-refinement loop (outer
+                              b - Ax in FP64) */
 
 /* Mesh set-up: the 'mesh' macro (Main.f:481-870): equation numbering
  * numeqpmec2 (Numeq.f:86-151), CSRD structure datastruct_pm/csrstruct_pm
@@ -116,7 +121,8 @@ int pm_get_csrd(pm_handle h, int64_t* ia, int32_t* ja, double* ad, double* al);
 int pm_assemble(pm_handle h, int isw, int lhs, int rhs, const double* u, double* b);
 
 /* matvec_csrc_sym_pm (Matvec.f:1504-1598): y = (D + L + L^T) x with the
- * assembled matrix.  x, y host arrays of length neq. */
+ * assembled matrix.  x, y host arrays of length neq.  Under PM_FP32C_REFINE
+ * the product is the compensated FP32 operator of the solver. */
 int pm_spmv(pm_handle h, const double* x, double* y);
 
 /* solv_pm (Solv.f:27-780): solver 1 = PCG (Iters.f:299-595),
@@ -166,9 +172,17 @@ int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* d_ja,
                         const double* d_ad, const double* d_al, const double* d_b,
                         double* d_x, double tol, int maxit, int* iters, void* stream);
 
+/* Autotuner of the PM_FP32C_REFINE SpMV (no counterpart in the reference,
+ * whose SpMV has no tunable shape): builds the compensated values of the
+ * assembled matrix if needed, times the kernel shapes (8, 16 or 32 lanes per
+ * node x 1, 2 or 4 columns per lane and trip) on it and keeps the fastest;
+ * *shape receives its code, 10 * (0, 1, 2 for 8, 16, 32 lanes) + columns.
+ * The first compensated solve or product runs it implicitly. */
+int pm_tune_spmv(pm_handle h, int* shape);
+
 /* Timing of the last pm_step phases in milliseconds (CUDA events):
  * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,
- * [3] solve, [4] updates, [5] SpMV kernel time of the solve (sum),
+ * [3] solve, [4] unused (0), [5] device time of the last Krylov solve,
  * [6] Krylov iterations of the last solve, [7] kernels launched by the step. */
 int pm_get_timers(pm_handle h, double* t, int n);
 

@@ -21,6 +21,7 @@ PM_PROP = 15
 PM_NFLOAD = 6
 PM_FP64 = 0
 PM_FP32_REFINE = 1
+PM_FP32C_REFINE = 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "element Jacobian determinant <= 1e-14",
           3: "zero diagonal coefficient", 4: "Krylov solver did not converge",
@@ -70,6 +71,7 @@ def load(path=None):
     lib.pm_set_initial_stress.argtypes = [c_p, c_p]
     lib.pm_set_precision.argtypes = [c_p, c_i]
     lib.pm_set_refine.argtypes = [c_p, c_d]
+    lib.pm_tune_spmv.argtypes = [c_p, ctypes.POINTER(ctypes.c_int)]
     lib.pm_get_sizes.argtypes = [c_p] * 5
     lib.pm_get_id.argtypes = [c_p, c_p]
     lib.pm_get_csrd.argtypes = [c_p] * 5
@@ -177,6 +179,14 @@ class Mesh:
 
     def set_refine(self, inner_tol=1e-5):
         self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
+
+    def tune_spmv(self):
+        """Autotune the compensated SpMV on the assembled matrix; returns the
+        chosen shape code: 10 * (0, 1, 2 for 8, 16, 32 lanes per node) +
+        columns per lane and trip."""
+        u = ctypes.c_int(0)
+        self._check(self.lib.pm_tune_spmv(self.h, ctypes.byref(u)), "pm_tune_spmv")
+        return u.value
 
     def get_id(self):
         idr = np.zeros((self.nnode, 4), np.int32)

@@ -182,7 +182,6 @@ int assemble_K(Handle* h, bool fp32) {
   if (fp32) {
     if (!h->P.val32) {
       PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
-      h->pcg_graph_val = h->minres_graph_val = nullptr;
       if (h->pcgm_graph) {
         cudaGraphExecDestroy(h->pcgm_graph);
         h->pcgm_graph = nullptr;
@@ -196,8 +195,12 @@ int assemble_K(Handle* h, bool fp32) {
   for (int c = 0; c < h->numcolors; ++c)
     PM_CUDA(pm::launch_assemble_K(elem_launch(h, c), h->hexa, fp32 ? nullptr : h->P.val,
                                   fp32 ? h->P.val32 : nullptr, h->stream));
-  if (fp32) h->assembled32 = true;
-  else h->assembled = true;
+  if (fp32) {
+    h->assembled32 = true;
+  } else {
+    h->assembled = true;
+    h->assembled32 = h->assembledC = false;
+  }
   h->assembled_dt = h->dt;
   return PM_OK;
 }
@@ -271,72 +274,145 @@ int capture(Handle* h, cudaGraphExec_t* exec, Body body) {
   return PM_OK;
 }
 
+// Runs graphs of kGraphIters iterations until the solve's flag is set.
+int run_graph(Handle* h, cudaGraphExec_t g, pm::KrylovScalars* ks) {
+  for (;;) {
+    PM_CUDA(cudaGraphLaunch(g, h->stream));
+    h->launches += 3 * kGraphIters;
+    PM_TRY(read_scalars(h, ks));
+    if (ks->conv_flag) return PM_OK;
+  }
+}
+
 // One Krylov solve of K x = b on the device (solv_pm, Solv.f:27-780).
-// val32 != nullptr runs the iteration with FP32 matrix values.
+//
+// comp = false: the reference's FP64 iteration on the FP64 panels.
+// comp = true (PM_FP32C_REFINE): the same recurrences with FP64 vectors,
+// scalars and dots, whose operator products run on the compensated FP32
+// values (pm_krylov.h), inside an FP64 iterative-refinement loop:
+//   PCG:    solve to the reference's test sqrt|(r, m r)| < tol sqrt|(b, m b)|;
+//           then r = b - A64 x in FP64; while sqrt|(r, m r)| is above that
+//           target, solve A dx = r to the same absolute target, x += dx.
+//   MINRES: a restart computes v = b - A64 x in FP64 (Iters.f:4100-4131), so
+//           a converged cycle is followed by one such restart whose FP64
+//           residual norm beta must also meet the target, else the cycle
+//           continues from there (within the reference's 10 restarts).
 int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, int maxit,
-           const float* val32, pm_step_info* info) {
+           bool comp, pm_step_info* info) {
   const int n = h->neq;
   pm::KrylovVecs& V = h->D.kv;
+  pm::KrylovVecs32& V32 = h->D.kv32;
   const pm::PanelView P = h->P.view();
-  // the FP64 solve runs on the FP64 panels; the FP32 operator has its own
-  // inner solver (refine)
   const double* val64 = h->P.val;
-  val32 = nullptr;
+  const pm::CompVals C{h->P.valh, h->P.vall, h->shape};
   pm::KrylovScalars ks{};
+  int sweeps = 0;
   cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
   PM_CUDA(cudaEventRecord(e0, h->stream));
   if (solver == 1) {
-    const void* vkey = val32 ? (const void*)val32 : (const void*)val64;
-    if (!h->pcg_graph || h->pcg_graph_val != vkey) {
-      PM_TRY(capture(h, &h->pcg_graph, [&]() {
-        return pm::pcg_iteration(P, val64, val32, n, h->D.m, V, h->D.ks, h->D.partial,
-                                 h->D.counter, h->stream);
+    cudaGraphExec_t* g = comp ? &h->pcgc_graph : &h->pcg_graph;
+    if (!*g) {
+      PM_TRY(capture(h, g, [&]() {
+        return comp ? pm::pcgc_iteration(P, C, n, h->D.m, V, V32, h->D.ks, h->D.partial,
+                                         h->D.counter, h->stream)
+                    : pm::pcg_iteration(P, val64, n, h->D.m, V, h->D.ks, h->D.partial,
+                                        h->D.counter, h->stream);
       }));
-      h->pcg_graph_val = vkey;
     }
     h->launches += 1;
-    PM_CUDA(pm::pcg_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
-                         h->stream));
-    for (;;) {
-      PM_CUDA(cudaGraphLaunch(h->pcg_graph, h->stream));
-      h->launches += 3 * kGraphIters;
-      PM_TRY(read_scalars(h, &ks));
-      if (ks.conv_flag) break;
+    if (comp)
+      PM_CUDA(pm::pcgc_init(n, d_b, h->D.m, V, V32, h->D.ks, tol, -1.0, maxit, h->D.partial,
+                            h->D.counter, h->stream));
+    else
+      PM_CUDA(pm::pcg_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
+                           h->stream));
+    PM_TRY(run_graph(h, *g, &ks));
+    int total = ks.iter;
+    const double conv = ks.conv;
+    const int kMaxSweeps = 8;
+    while (comp && ks.conv_flag == 1) {
+      // x (d_x) += dx (V.x); r = b - A64 x; stop when |r| meets the target
+      h->launches += 3;
+      if (sweeps == 0) {
+        if (d_x != V.x)
+          PM_CUDA(cudaMemcpyAsync(d_x, V.x, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                  h->stream));
+      } else {
+        PM_CUDA(pm::axpy_into(n, d_x, V.x, 1.0, h->stream));
+      }
+      PM_CUDA(pm::spmv(P, val64, d_x, h->D.dx, 0, nullptr, nullptr, nullptr, h->stream));
+      PM_CUDA(pm::true_residual(n, d_b, h->D.dx, h->D.m, 0, h->D.rr, h->D.norms, h->D.partial,
+                                h->D.counter, h->stream));
+      double rn2 = 0.0;
+      PM_CUDA(cudaMemcpyAsync(&rn2, h->D.norms, sizeof(double), cudaMemcpyDeviceToHost,
+                              h->stream));
+      PM_CUDA(cudaStreamSynchronize(h->stream));
+      ++sweeps;
+      if (h->debug)
+        fprintf(stderr, "refine sweep %d: |b-A64x| %.3e target %.3e after %d its\n", sweeps,
+                std::sqrt(std::fabs(rn2)), conv, total);
+      if (std::sqrt(std::fabs(rn2)) < conv) break;
+      if (sweeps >= kMaxSweeps || total >= maxit) {
+        ks.conv_flag = 2;
+        break;
+      }
+      h->launches += 1;
+      PM_CUDA(pm::pcgc_init(n, h->D.rr, h->D.m, V, V32, h->D.ks, tol, conv, maxit - total,
+                            h->D.partial, h->D.counter, h->stream));
+      PM_TRY(run_graph(h, *g, &ks));
+      total += ks.iter;
     }
+    ks.iter = total;
     if (ks.conv_flag != 1) {
       h->err = ks.conv_flag == 3
                    ? "PCG: breakdown (non-finite recurrence) after " + std::to_string(ks.iter) +
                          " iterations"
-                   : "PCG: no convergence reached after " + std::to_string(maxit) + " iterations";
+                   : "PCG: no convergence reached after " + std::to_string(ks.iter) +
+                         " iterations";
       if (info) info->iters = ks.iter;
       return PM_E_NOCONV;
     }
   } else if (solver == 7) {
-    const void* vkey = val32 ? (const void*)val32 : (const void*)val64;
-    if (!h->minres_graph || h->minres_graph_val != vkey) {
-      PM_TRY(capture(h, &h->minres_graph, [&]() {
-        return pm::minres_iteration(P, val64, val32, n, h->D.m, V, h->D.ks, h->D.partial,
-                                    h->D.counter, h->stream);
+    cudaGraphExec_t* g = comp ? &h->minresc_graph : &h->minres_graph;
+    if (!*g) {
+      PM_TRY(capture(h, g, [&]() {
+        return comp ? pm::minresc_iteration(P, C, n, h->D.m, V, V32, h->D.ks, h->D.partial,
+                                            h->D.counter, h->stream)
+                    : pm::minres_iteration(P, val64, n, h->D.m, V, h->D.ks, h->D.partial,
+                                           h->D.counter, h->stream);
       }));
-      h->minres_graph_val = vkey;
     }
     PM_CUDA(cudaMemsetAsync(h->D.ks, 0, sizeof(pm::KrylovScalars), h->stream));
     PM_CUDA(pm::minres_conv(n, d_b, h->D.m, h->D.ks, tol, h->D.partial, h->D.counter,
                             h->stream));
     int nrestart = 10;  // call_minres, Solv.f:1727
-    bool zero_x = true;
+    bool zero_x = true, converged = false;
     for (;;) {
       h->launches += zero_x ? 1 : 2;
-      PM_CUDA(pm::minres_start(P, val64, val32, n, d_b, h->D.m, V, h->D.ks, maxit, zero_x,
-                               h->D.partial, h->D.counter, h->stream));
-      zero_x = false;
-      for (;;) {
-        PM_CUDA(cudaGraphLaunch(h->minres_graph, h->stream));
-        h->launches += 3 * kGraphIters;
+      PM_CUDA(pm::minres_start(P, val64, n, d_b, h->D.m, V, comp ? &V32 : nullptr, h->D.ks,
+                               maxit, zero_x, h->D.partial, h->D.counter, h->stream));
+      if (converged) {
+        // the FP64 residual of the converged compensated cycle
         PM_TRY(read_scalars(h, &ks));
-        if (ks.conv_flag) break;
+        ++sweeps;
+        if (h->debug)
+          fprintf(stderr, "refine sweep %d: |b-A64x| %.3e target %.3e after %d its\n", sweeps,
+                  ks.beta, ks.conv, ks.iter);
+        if (ks.beta < ks.conv) break;
+        if (sweeps >= 8) {
+          h->err = "MINRES: the FP64 residual stayed above the target after " +
+                   std::to_string(sweeps) + " refinement sweeps";
+          if (info) info->iters = ks.iter;
+          return PM_E_NOCONV;
+        }
       }
-      if (ks.conv_flag == 1) break;
+      zero_x = false;
+      PM_TRY(run_graph(h, *g, &ks));
+      if (ks.conv_flag == 1) {
+        if (!comp) break;
+        converged = true;
+        continue;
+      }
       if (ks.conv_flag == 3) {
         h->err = "MINRES: breakdown (non-finite recurrence) after " + std::to_string(ks.iter) +
                  " iterations";
@@ -356,18 +432,20 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   }
   PM_CUDA(cudaEventRecord(e1, h->stream));
   // x.Kx of the solver log (one more product with the converged x)
+  const double* xs = (comp && solver == 1) ? d_x : V.x;
   h->launches += 1;
-  PM_CUDA(pm::spmv(P, val64, val32, V.x, V.q, 3, h->D.ks, h->D.partial, h->D.counter,
-                   h->stream));
-  if (d_x != V.x)
-    PM_CUDA(cudaMemcpyAsync(d_x, V.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  PM_CUDA(pm::spmv(P, val64, xs, V.q, 3, h->D.ks, h->D.partial, h->D.counter, h->stream));
+  if (d_x != xs)
+    PM_CUDA(cudaMemcpyAsync(d_x, xs, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+  const int iters = ks.iter;
   PM_TRY(read_scalars(h, &ks));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
   h->timers[5] = ms;
-  h->timers[6] = ks.iter;
+  h->timers[6] = iters;
   if (info) {
-    info->iters = ks.iter;
+    info->iters = iters;
+    info->refine = sweeps;
     info->conv = ks.conv;
     info->xkx = ks.xkx;
   }
@@ -447,8 +525,7 @@ int solve_mixed(Handle* h, int solver, const double* d_b, double* d_x, double to
     // x += dx;  r = b - A64 x
     h->launches += 3;
     PM_CUDA(pm::axpy_into(n, d_x, V.x, 1.0, h->stream));
-    PM_CUDA(pm::spmv(P, h->P.val, nullptr, d_x, h->D.by, 0, nullptr, nullptr, nullptr,
-                     h->stream));
+    PM_CUDA(pm::spmv(P, h->P.val, d_x, h->D.by, 0, nullptr, nullptr, nullptr, h->stream));
     PM_CUDA(pm::vsub(n, r, d_b, h->D.by, h->stream));
   }
   if (sweep == kMaxSweeps) {
@@ -466,6 +543,74 @@ int solve_mixed(Handle* h, int solver, const double* d_b, double* d_x, double to
     info->refine = sweep;
     info->conv = tol * bnorm;
   }
+  return PM_OK;
+}
+
+// Autotuner of the compensated SpMV: times each shape (lanes per node 8, 16,
+// 32 x columns per lane and trip 1, 2, 4) on this matrix, 3 launches each
+// after one warm-up, with CUDA events on the launching stream, and keeps the
+// fastest for the handle's lifetime (graphs captured later bake it in).
+// PM_SPMV_SHAPE=<code> in the environment fixes the choice instead.
+int tune_spmvc(Handle* h, cudaStream_t s) {
+  if (h->shape) return PM_OK;
+  if (const char* env = std::getenv("PM_SPMV_SHAPE")) {
+    const int u = std::atoi(env);
+    for (int c : pm::kCfShapes)
+      if (u == c) {
+        h->shape = u;
+        return PM_OK;
+      }
+  }
+  const pm::PanelView P = h->P.view();
+  PM_CUDA(cudaMemsetAsync(h->D.kv32.c, 0, sizeof(float2) * std::max(h->neq, 1), s));
+  float best = 0.f;
+  int best_c = 1;
+  for (int c : pm::kCfShapes) {
+    const pm::CompVals C{h->P.valh, h->P.vall, c};
+    PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
+    PM_CUDA(cudaEventRecord(h->ev[0], s));
+    for (int k = 0; k < 3; ++k) PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
+    PM_CUDA(cudaEventRecord(h->ev[1], s));
+    PM_CUDA(cudaEventSynchronize(h->ev[1]));
+    float ms = 0.f;
+    PM_CUDA(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+    if (h->debug) fprintf(stderr, "spmv autotune: shape %2d  %.4f ms\n", c, ms / 3);
+    if (c == pm::kCfShapes[0] || ms < best) {
+      best = ms;
+      best_c = c;
+    }
+    h->launches += 4;
+  }
+  h->shape = best_c;
+  return PM_OK;
+}
+
+// Compensated copies of the current FP64 panel values (PM_FP32C_REFINE).
+int ensure_comp(Handle* h, cudaStream_t s) {
+  if (h->assembledC) return PM_OK;
+  if (!h->P.valh) {
+    PM_CUDA(cudaMalloc(&h->P.valh, sizeof(float) * (size_t)h->P.nnz));
+    PM_CUDA(cudaMalloc(&h->P.vall, sizeof(int8_t) * (size_t)h->P.nnz));
+  }
+  h->launches += 1;
+  PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
+  h->assembledC = true;
+  return tune_spmvc(h, s);
+}
+
+// y = A x by the handle's operator: FP64 panels, or in PM_FP32C_REFINE the
+// compensated one (x split into its FP32 pair first).
+int spmv_op(Handle* h, const double* d_x, double* d_y, cudaStream_t s) {
+  if (h->precision == PM_FP32C_REFINE) {
+    PM_TRY(ensure_comp(h, s));
+    h->launches += 2;
+    PM_CUDA(pm::split_pair(h->neq, d_x, h->D.kv32.c, s));
+    PM_CUDA(pm::spmvc(h->P.view(), pm::CompVals{h->P.valh, h->P.vall, h->shape}, h->D.kv32.c,
+                      d_y, s));
+    return PM_OK;
+  }
+  h->launches += 1;
+  PM_CUDA(pm::spmv(h->P.view(), h->P.val, d_x, d_y, 0, nullptr, nullptr, nullptr, s));
   return PM_OK;
 }
 
@@ -491,7 +636,11 @@ int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x
     }
     return solve_mixed(h, solver, d_b, d_x, tol, maxit, info);
   }
-  return krylov(h, solver, d_b, d_x, tol, maxit, nullptr, info);
+  if (h->precision == PM_FP32C_REFINE) {
+    PM_TRY(ensure_comp(h, h->stream));
+    return krylov(h, solver, d_b, d_x, tol, maxit, true, info);
+  }
+  return krylov(h, solver, d_b, d_x, tol, maxit, false, info);
 }
 
 int alloc_state(Handle* h) {
@@ -532,6 +681,10 @@ int alloc_state(Handle* h) {
     }
     cudaMemset(*p, 0, sizeof(float) * std::max<size_t>(n, 1));
   }
+  if (cudaMalloc((void**)&V32.c, sizeof(float2) * std::max<size_t>(n, 1)) != cudaSuccess) {
+    h->err = "cudaMalloc failed";
+    return PM_E_NOMEM;
+  }
   PM_TRY(A(&D.partial, 4 * (size_t)pm::kRedBlocks));
   PM_CUDA(cudaMalloc(&D.counter, sizeof(unsigned) * 4));
   PM_CUDA(cudaMemset(D.counter, 0, sizeof(unsigned) * 4));
@@ -549,14 +702,16 @@ void free_all(Handle* h) {
                   D.ad, D.m, D.bx, D.by, D.rr, D.dx, D.xs, D.kv.x, D.kv.r, D.kv.z, D.kv.p, D.kv.q,
                   D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
-                  P.val32, P.node_val_off, P.node_W, P.order};
+                  P.val32, P.valh, P.vall, P.node_val_off, P.node_W, P.order};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q})
+  for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})
     if (p) cudaFree(p);
   if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
   if (h->pcgm_graph) cudaGraphExecDestroy(h->pcgm_graph);
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
+  if (h->pcgc_graph) cudaGraphExecDestroy(h->pcgc_graph);
+  if (h->minresc_graph) cudaGraphExecDestroy(h->minresc_graph);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -583,7 +738,7 @@ int upload_materials(Handle* h) {
   if (!h->D.mat) PM_CUDA(cudaMalloc(&h->D.mat, sizeof(pm::MatConst) * h->numat));
   PM_CUDA(cudaMemcpy(h->D.mat, h->h_mat.data(), sizeof(pm::MatConst) * h->numat,
                      cudaMemcpyHostToDevice));
-  h->assembled = h->assembled32 = false;
+  h->assembled = h->assembled32 = h->assembledC = false;
   return PM_OK;
 }
 
@@ -706,7 +861,7 @@ int pm_set_env(pm_handle hh, const double* gravity, double dt, double t, int ist
                                gravity[2] * gravity[2]);
     PM_TRY(upload_materials(h));
   }
-  if (dt != h->dt) h->assembled = h->assembled32 = false;
+  if (dt != h->dt) h->assembled = h->assembled32 = h->assembledC = false;
   h->dt = dt;
   h->t = t;
   h->istep = istep;
@@ -758,8 +913,21 @@ int pm_set_initial_stress(pm_handle hh, const double* tx0) {
 
 int pm_set_precision(pm_handle hh, int mode) {
   Handle* h = reinterpret_cast<Handle*>(hh);
-  if (!h || (mode != PM_FP64 && mode != PM_FP32_REFINE)) return PM_E_ARG;
+  if (!h || (mode != PM_FP64 && mode != PM_FP32_REFINE && mode != PM_FP32C_REFINE))
+    return PM_E_ARG;
   h->precision = mode;
+  return PM_OK;
+}
+
+int pm_tune_spmv(pm_handle hh, int* shape) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !shape) return PM_E_ARG;
+  if (!h->assembled) {
+    h->err = "matrix not assembled";
+    return PM_E_STATE;
+  }
+  PM_TRY(ensure_comp(h, h->stream));
+  *shape = h->shape;
   return PM_OK;
 }
 
@@ -850,8 +1018,7 @@ int pm_spmv_dev(pm_handle hh, const double* d_x, double* d_y, void* stream) {
     return PM_E_STATE;
   }
   cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
-  PM_CUDA(pm::spmv(h->P.view(), h->P.val, nullptr, d_x, d_y, 0, nullptr, nullptr, nullptr, s));
-  return PM_OK;
+  return spmv_op(h, d_x, d_y, s);
 }
 
 int pm_spmv(pm_handle hh, const double* x, double* y) {
@@ -862,8 +1029,7 @@ int pm_spmv(pm_handle hh, const double* x, double* y) {
     return PM_E_STATE;
   }
   PM_CUDA(cudaMemcpyAsync(h->D.bx, x, sizeof(double) * h->neq, cudaMemcpyHostToDevice, h->stream));
-  PM_CUDA(pm::spmv(h->P.view(), h->P.val, nullptr, h->D.bx, h->D.by, 0, nullptr, nullptr,
-                   nullptr, h->stream));
+  PM_TRY(spmv_op(h, h->D.bx, h->D.by, h->stream));
   PM_CUDA(cudaMemcpyAsync(y, h->D.by, sizeof(double) * h->neq, cudaMemcpyDeviceToHost, h->stream));
   PM_CUDA(cudaStreamSynchronize(h->stream));
   return PM_OK;
@@ -942,7 +1108,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
     const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
     if (need_K) {
       PM_TRY(assemble_K(h, false));
-      h->assembled32 = false;
+      h->assembled32 = h->assembledC = false;
     }
     PM_CUDA(cudaEventRecord(ev[3], s));
     PM_TRY(residual(h, D.u, D.b));

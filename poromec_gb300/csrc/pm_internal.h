@@ -46,6 +46,8 @@ struct Panels {
   int32_t* cols = nullptr;
   double* val = nullptr;   // FP64 values
   float* val32 = nullptr;  // FP32 values (PM_FP32_REFINE)
+  float* valh = nullptr;      // compensated values (PM_FP32C_REFINE): fl32(v)
+  int8_t* vall = nullptr;     //   and round((v - fl32(v)) / fl32(v) * 2^31)
   // indexed by node id - 1
   int64_t* node_val_off = nullptr;
   int32_t* node_W = nullptr;
@@ -139,16 +141,18 @@ struct Handle {
   bool fstress0 = false;
   bool assembled = false;      // FP64 panel values valid
   bool assembled32 = false;    // FP32 panel values valid
+  bool assembledC = false;     // compensated panel values valid
+  int shape = 0;               // compensated SpMV shape code (0 = not tuned)
   double assembled_dt = -1.0;
   double resu0 = 0.0, resp0 = 0.0, res0 = 0.0;
   Panels P;
   Dev D;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  // graphs of kGraphIters iterations (pointers baked in are fixed for the
+  // handle's lifetime)
   cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr, pcgm_graph = nullptr;
-  const void* pcg_graph_val = nullptr;   // values pointer baked into the graph
-  const void* minres_graph_val = nullptr;
-  const double* pcg_graph_m = nullptr;
+  cudaGraphExec_t pcgc_graph = nullptr, minresc_graph = nullptr;
   double timers[8] = {0};
   int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;

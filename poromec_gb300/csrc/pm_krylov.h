@@ -41,9 +41,11 @@ struct KrylovVecs {
 };
 
 // FP32 copies used by the mixed-precision PCG: the search direction and
-// its product with the FP32 matrix.
+// its product with the FP32 matrix (PM_FP32_REFINE); the operand of the
+// compensated product as interleaved (hi, lo) pairs (PM_FP32C_REFINE).
 struct KrylovVecs32 {
   float *p, *q;
+  float2* c;
 };
 
 int vec_grid(int n);
@@ -53,24 +55,25 @@ cudaError_t pcgm_init(int n, const double* b, const double* m, KrylovVecs& V,
 cudaError_t pcgm_iteration(const PanelView& P, const float* val32, int n, const double* m,
                            KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
                            double* partial, unsigned* counter, cudaStream_t s);
-cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
-                 const double* x, double* y, int mode, KrylovScalars* ks,
-                 double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t spmv(const PanelView& P, const double* val64, const double* x, double* y,
+                 int mode, KrylovScalars* ks, double* partial, unsigned* counter,
+                 cudaStream_t s);
 cudaError_t pcg_init(int n, const double* b, const double* m, KrylovVecs& V,
                      KrylovScalars* ks, double tol, int maxit, double* partial,
                      unsigned* counter, cudaStream_t s);
-cudaError_t pcg_iteration(const PanelView& P, const double* val64, const float* val32,
-                          int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
-                          double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t pcg_iteration(const PanelView& P, const double* val64, int n, const double* m,
+                          KrylovVecs& V, KrylovScalars* ks, double* partial,
+                          unsigned* counter, cudaStream_t s);
 cudaError_t minres_conv(int n, const double* b, const double* m, KrylovScalars* ks,
                         double tol, double* partial, unsigned* counter, cudaStream_t s);
-cudaError_t minres_start(const PanelView& P, const double* val64, const float* val32,
-                         int n, const double* b, const double* m, KrylovVecs& V,
+// pair != nullptr also writes the FP32 pair of z0 (compensated iteration)
+cudaError_t minres_start(const PanelView& P, const double* val64, int n, const double* b,
+                         const double* m, KrylovVecs& V, const KrylovVecs32* pair,
                          KrylovScalars* ks, int maxit, bool zero_x, double* partial,
                          unsigned* counter, cudaStream_t s);
-cudaError_t minres_iteration(const PanelView& P, const double* val64, const float* val32,
-                             int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
-                             double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t minres_iteration(const PanelView& P, const double* val64, int n, const double* m,
+                             KrylovVecs& V, KrylovScalars* ks, double* partial,
+                             unsigned* counter, cudaStream_t s);
 cudaError_t csrd_spmv(int neq, const int64_t* ia, const int32_t* ja, const double* ad,
                       const double* al, const double* x, double* y, cudaStream_t s);
 cudaError_t precond(int n, const double* ad, double* m, int absval, int* zero_diag,
@@ -84,5 +87,33 @@ cudaError_t wnorm2(int n, const double* r, const double* m, double* out, double*
 cudaError_t axpy_into(int n, double* y, const double* x, double a, cudaStream_t s);
 cudaError_t vsub(int n, double* y, const double* a, const double* b, cudaStream_t s);
 cudaError_t to_f32(int64_t n, const double* a, float* b, cudaStream_t s);
+
+// Compensated FP32 operator (PM_FP32C_REFINE).  Each FP64 panel value v is
+// held as hi = fl32(v) and an int8 relative correction q (v = hi (1 + q 2^-31)
+// within 2^-32 |v|), 5 bytes; the operand vector as interleaved FP32 pairs
+// (KrylovVecs32::c); products and sums in compensated FP32 arithmetic, the
+// result in FP64.
+struct CompVals {
+  const float* hi;
+  const int8_t* lo;
+  int shape;  // SpMV shape: 10 * (0: 8, 1: 16, 2: 32 lanes per node) + columns
+              // per lane and trip (1, 2, 4)
+};
+constexpr int kCfShapes[] = {1, 2, 4, 11, 12, 14, 21, 22, 24};
+cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
+cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s);
+cudaError_t spmvc(const PanelView& P, CompVals C, const float2* xp, double* y, cudaStream_t s);
+cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,
+                      KrylovVecs32& V32, KrylovScalars* ks, double tol, double conv_abs,
+                      int maxit, double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t pcgc_iteration(const PanelView& P, CompVals C, int n, const double* m,
+                           KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                           double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const double* m,
+                              KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                              double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t true_residual(int n, const double* b, const double* q, const double* m, int absval,
+                          double* r, double* out, double* partial, unsigned* counter,
+                          cudaStream_t s);
 
 }  // namespace pm

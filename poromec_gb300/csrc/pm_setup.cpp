@@ -158,13 +158,28 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
     h->h_d[k] = dn[n];
     h->h_W[k] = Wn[n];
     h->h_low[k] = lown[n];
+    node_W[n] = Wn[n];
+    for (int q = 0; q < dn[n]; ++q) nad += lown[n] + q;
+  }
+  // SpMV visiting order: by free dofs, then panel width (descending), then
+  // equation order, so the nodes sharing a warp run identical loops.  The
+  // panels and their column lists are stored in this order, so the SpMV
+  // streams them sequentially (a scattered visit over GBs of panels costs
+  // DRAM pages and TLB reach).
+  std::vector<int32_t> order(nact);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
+    return h->h_W[a] > h->h_W[b];
+  });
+  for (int i = 0; i < nact; ++i) {
+    const int k = order[i];
+    const int n = act[k];
     h->h_val_off[k] = vo;
     h->h_col_off[k] = co;
     node_val_off[n] = vo;
-    node_W[n] = Wn[n];
     vo += (int64_t)dn[n] * Wn[n];
     co += Wn[n];
-    for (int q = 0; q < dn[n]; ++q) nad += lown[n] + q;
   }
   h->h_val_off[nact] = vo;
   h->h_col_off[nact] = co;
@@ -239,14 +254,6 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
   P.nnz = vo;
   P.ncols = co;
   int st;
-  // SpMV visiting order: by free dofs, then panel width (descending), then
-  // equation order, so the nodes sharing a warp run identical loops
-  std::vector<int32_t> order(nact);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
-    return h->h_W[a] > h->h_W[b];
-  });
   if ((st = upload(h, &P.order, order.data(), nact))) return st;
   if ((st = upload(h, &P.eq0, h->h_eq0.data(), nact))) return st;
   if ((st = upload(h, &P.d, h->h_d.data(), nact))) return st;

@@ -86,6 +86,14 @@ __device__ __forceinline__ bool krylov_skip(KrylovScalars* ks, bool first) {
   return false;
 }
 
+// v as an unevaluated FP32 pair (hi, lo), |v - hi - lo| <= 2^-48 |v|: the
+// operand format of the compensated operator, interleaved so that one 8-byte
+// gather fetches both halves.
+__device__ __forceinline__ void split_store(double v, float2* pr, int i) {
+  const float h = float(v);
+  pr[i] = make_float2(h, float(v - double(h)));
+}
+
 // ---- SpMV over panels ------------------------------------------------------
 // A sub-warp of 8 lanes per node: lane t of the sub-warp accumulates columns
 // t, t+8, ... of the node's d <= 4 panel rows (coalesced 64-byte runs per
@@ -375,7 +383,7 @@ __global__ void __launch_bounds__(256)
                    const double* __restrict__ m, double* __restrict__ v,
                    double* __restrict__ v0, double* __restrict__ w0,
                    double* __restrict__ w00, double* __restrict__ z0, KrylovScalars* ks,
-                   int maxit, double* partial, unsigned* counter) {
+                   int maxit, double* partial, unsigned* counter, float2* __restrict__ zc) {
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double vi = b[i] - q[i];
@@ -385,6 +393,7 @@ __global__ void __launch_bounds__(256)
     w00[i] = 0.0;
     const double zi = vi * m[i];
     z0[i] = zi;
+    if (zc) split_store(zi, zc, i);
     acc += vi * zi;
   }
   double in[1] = {acc}, tot[1];
@@ -412,7 +421,7 @@ __global__ void __launch_bounds__(256)
     k_minres_lanczos(int n, double* __restrict__ p, const double* __restrict__ v,
                      const double* __restrict__ v0, const double* __restrict__ m,
                      double* __restrict__ z, KrylovScalars* ks, double* partial,
-                     unsigned* counter) {
+                     unsigned* counter, float2* __restrict__ zc) {
   if (krylov_skip(ks, false)) return;
   const double beta = ks->beta;
   const double t1 = 1.0 / beta, t2 = -ks->alpha / beta, t3 = -beta / ks->beta_old;
@@ -422,6 +431,7 @@ __global__ void __launch_bounds__(256)
     p[i] = pi;
     const double zi = pi * m[i];
     z[i] = zi;
+    if (zc) split_store(zi, zc, i);
     acc += zi * pi;
   }
   double in[1] = {acc}, tot[1];
@@ -480,6 +490,244 @@ __global__ void __launch_bounds__(256)
     w00[i] = w0[i];
     w0[i] = wi;
   }
+}
+
+// ---- compensated FP32 operator (PM_FP32C_REFINE) -----------------------------
+// Each FP64 panel value v is stored as hi = fl32(v) and an int8 relative
+// correction q = round((v - hi) / hi * 2^31), |q| <= 127 (5 bytes; v is
+// represented as hi (1 + q 2^-31) within 2^-32 |v|, hi's own rounding being
+// at most 2^-24 |hi|).  The operand vector is an FP32 pair (xh, xl).
+// Products and sums use error-free FP32 transformations: t = hi*xh and its
+// rounding error e = fma(hi, xh, -t) (TwoProd), the cross terms hi*xl and
+// t*q*2^-31 (= (v - hi)*xh to 2^-24 relative) go to a correction, and the
+// running sum is a (sum, correction) pair updated with TwoSum.  The FP32
+// pipe issues 128 lanes per clock per SM against 2 for FP64, so this
+// operator is bound by HBM, with an error of ~2e-10 per entry where plain
+// FP32 storage (2^-24) is amplified by the conditioning of this indefinite
+// system beyond what refinement recovers.
+struct F2 {
+  float s, c;
+};
+
+__device__ __forceinline__ void two_sum_acc(F2& a, float t) {
+  const float s = a.s + t;
+  const float bp = s - a.s;
+  const float err = (a.s - (s - bp)) + (t - bp);
+  a.s = s;
+  a.c += err;
+}
+
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  F2 r{a.s, a.c + b.c};
+  two_sum_acc(r, b.s);
+  return r;
+}
+
+// q * 2^-31 for an int8 q, exactly: 1.5 * 2^23 + q is a float whose low
+// mantissa bits are q; scaling by 2^-31 and removing 1.5 * 2^-8 is exact.
+__device__ __forceinline__ float q_scale(int q) {
+  return fmaf(__int_as_float(0x4B400000 + q), 0x1p-31f, -0x1.8p-8f);
+}
+
+__device__ __forceinline__ void f2_fma(F2& acc, float vh, int q, float xh, float xl) {
+  const float t = vh * xh;
+  const float e = fmaf(vh, xh, -t);
+  const float c = fmaf(vh, xl, fmaf(t, q_scale(q), e));
+  two_sum_acc(acc, t);
+  acc.c += c;
+}
+
+__device__ __forceinline__ F2 f2_shfl(F2 a, int m) {
+  return F2{__shfl_xor_sync(0xffffffffu, a.s, m), __shfl_xor_sync(0xffffffffu, a.c, m)};
+}
+
+// Rows of one node panel on the compensated operator: lane t of the S-lane
+// sub-warp takes columns t, t + S, ...; U columns per trip.  The column
+// indices of the next trip are loaded one trip ahead, so each trip issues its
+// U gathers of x pairs together with its U * D value loads instead of after
+// a dependent index load.  Values and column indices are read once per
+// product and loaded with the evict-first hint, which leaves L2 to the
+// gathered operand.  The last trip is masked.
+template <int D, int S, int U>
+__device__ __forceinline__ void cf_rows(const float* __restrict__ h,
+                                        const int8_t* __restrict__ l,
+                                        const int32_t* __restrict__ cols,
+                                        const float2* __restrict__ xp, int W, int t,
+                                        F2 (&a)[4]) {
+  int cn[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) cn[u] = (t + u * S < W) ? __ldcs(&cols[t + u * S]) : -1;
+  for (int c = t; c < W; c += U * S) {
+    float2 xv[U];
+    float hv[U][D];
+    int lv[U][D];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xv[u] = cn[u] >= 0 ? xp[cn[u]] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        const bool ok = c + u * S < W;
+        hv[u][r] = ok ? __ldcs(&h[r * W + c + u * S]) : 0.f;
+        lv[u][r] = ok ? int(__ldcs(&l[r * W + c + u * S])) : 0;
+      }
+    const int cnext = c + U * S;
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      cn[u] = (cnext + u * S < W) ? __ldcs(&cols[cnext + u * S]) : -1;
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int r = 0; r < D; ++r)
+        f2_fma(a[r], hv[u][r], lv[u][r], xv[u].x, xv[u].y);
+  }
+}
+
+// MODE 0: y = A x.  MODE 1: PCG, alpha = d / (y . xd).  MODE 2: MINRES,
+// alpha = |xd . y| / beta^2.  xd is the FP64 operand whose pair is xp; y is
+// FP64.  S: lanes per node (8, 16 or 32), U: columns per lane and trip; both
+// chosen per matrix by the autotuner.  With S = 32 a warp reads each panel
+// row as full 128-byte lines; with S = 8 four nodes share a warp and each
+// load instruction touches four lines.
+template <int MODE, int S, int U>
+__global__ void __launch_bounds__(256)
+    k_spmv_cf(PanelView P, const float* __restrict__ vh, const int8_t* __restrict__ vl,
+              const float2* __restrict__ xp, double* __restrict__ y, const double* __restrict__ xd,
+              KrylovScalars* ks, double* partial, unsigned* counter) {
+  if (MODE != 0)
+    if (krylov_skip(ks, true)) return;
+  const int lane = threadIdx.x & 31;
+  const int t = lane & (S - 1);
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
+  constexpr int kNodesPerWarp = 32 / S;
+  double dsum = 0.0;
+  for (int base = warp * kNodesPerWarp; base < P.nact; base += nwarp * kNodesPerWarp) {
+    const int slot = base + lane / S;
+    const int node = slot < P.nact ? P.order[slot] : 0;
+    int e0 = 0, d = 0, W = 0;
+    F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    if (slot < P.nact) {
+      e0 = P.eq0[node];
+      d = P.d[node];
+      W = P.W[node];
+      const int64_t vo = P.val_off[node];
+      const float* h = vh + vo;
+      const int8_t* l = vl + vo;
+      const int32_t* cols = P.cols + P.col_off[node];
+      if (d == 4) cf_rows<4, S, U>(h, l, cols, xp, W, t, a);
+      else if (d == 3) cf_rows<3, S, U>(h, l, cols, xp, W, t, a);
+      else if (d == 2) cf_rows<2, S, U>(h, l, cols, xp, W, t, a);
+      else cf_rows<1, S, U>(h, l, cols, xp, W, t, a);
+    }
+    // transposed butterfly on (sum, correction) pairs over the S lanes: the
+    // first two levels halve the rows each lane carries, the rest add
+    constexpr int o1 = S / 2, o2 = S / 4;
+    const bool h1 = (t & o1) != 0, h2 = (t & o2) != 0;
+    F2 k0 = h1 ? a[2] : a[0], k1 = h1 ? a[3] : a[1];
+    k0 = f2_add(k0, f2_shfl(h1 ? a[0] : a[2], o1));
+    k1 = f2_add(k1, f2_shfl(h1 ? a[1] : a[3], o1));
+    F2 k = h2 ? k1 : k0;
+    k = f2_add(k, f2_shfl(h2 ? k0 : k1, o2));
+#pragma unroll
+    for (int o = S / 8; o > 0; o >>= 1) k = f2_add(k, f2_shfl(k, o));
+    const int r = (h1 ? 2 : 0) + (h2 ? 1 : 0);
+    if ((t & (o2 - 1)) == 0 && r < d) {
+      const double v = double(k.s) + double(k.c);
+      y[e0 + r] = v;
+      if (MODE != 0) dsum += v * xd[e0 + r];
+    }
+  }
+  if (MODE != 0) {
+    double in[1] = {dsum}, tot[1];
+    if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+      if (MODE == 1) {
+        ks->pq = tot[0];
+        ks->alpha = ks->d / tot[0];
+      } else {
+        ks->alpha = fabs(tot[0]) * (1.0 / (ks->beta * ks->beta));
+      }
+    }
+  }
+}
+
+// FP64 panel values -> (hi = fl32(v), q = round((v - hi) / hi * 2^31)),
+// |q| clamped to 127 (a tie at the rounding bound costs one unit, 2^-31).
+__global__ void k_split_values(int64_t n, const double* __restrict__ v, float* __restrict__ hi,
+                               int8_t* __restrict__ lo) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double a = v[i];
+    const float h = float(a);
+    hi[i] = h;
+    double q = 0.0;
+    if (h != 0.f && isfinite(h)) q = rint((a - double(h)) / double(h) * 2147483648.0);
+    lo[i] = (int8_t)fmin(fmax(q, -127.0), 127.0);
+  }
+}
+
+__global__ void k_split_pair(int n, const double* __restrict__ v, float2* __restrict__ pr) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    split_store(v[i], pr, i);
+}
+
+// PCG start on the compensated operator: x = 0, r = b, z = m r, p = z (with
+// its FP32 pair), d = (r, z); conv = tol sqrt|d| as in pcg, or conv_abs when
+// positive (a refinement sweep aims at the first sweep's absolute target).
+__global__ void __launch_bounds__(256)
+    k_pcgc_init(int n, const double* __restrict__ b, const double* __restrict__ m,
+                double* __restrict__ r, double* __restrict__ z, double* __restrict__ p,
+                float2* __restrict__ pc, double* __restrict__ x,
+                KrylovScalars* ks, double tol, double conv_abs, int maxit, double* partial,
+                unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double bi = b[i], zi = bi * m[i];
+    x[i] = 0.0;
+    r[i] = bi;
+    z[i] = zi;
+    p[i] = zi;
+    split_store(zi, pc, i);
+    acc += bi * zi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    ks->d = tot[0];
+    ks->bmb = tot[0];
+    ks->conv = conv_abs > 0.0 ? conv_abs : tol * sqrt(fabs(tot[0]));
+    ks->done = 0;
+    ks->conv_flag = 0;
+    ks->iter = 0;
+    ks->maxit = maxit;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_pcgc_dir(int n, const double* __restrict__ z, double* __restrict__ p,
+               float2* __restrict__ pc, KrylovScalars* ks) {
+  if (krylov_skip(ks, false)) return;
+  const double beta = ks->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double pi = z[i] + beta * p[i];
+    p[i] = pi;
+    split_store(pi, pc, i);
+  }
+}
+
+// The FP64 outer residual of the refinement: r = b - q (q = A x by the FP64
+// operator) and out = (r, m r), with |m| when absval.
+__global__ void __launch_bounds__(256)
+    k_true_residual(int n, const double* __restrict__ b, const double* __restrict__ q,
+                    const double* __restrict__ m, int absval, double* __restrict__ r,
+                    double* out, double* partial, unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = b[i] - q[i];
+    r[i] = ri;
+    acc += ri * ri * (absval ? fabs(m[i]) : m[i]);
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) out[0] = tot[0];
 }
 
 // ---- reference CSRD layout --------------------------------------------------
@@ -582,10 +830,9 @@ int vec_grid(int n) {
   return g < 1 ? 1 : (g > kRedBlocks ? kRedBlocks : g);
 }
 
-cudaError_t spmv(const PanelView& P, const double* val64, const float* val32,
-                 const double* x, double* y, int mode, KrylovScalars* ks,
-                 double* partial, unsigned* counter, cudaStream_t s) {
-  (void)val32;  // the FP32 operator runs on FP32 vectors: spmv32
+cudaError_t spmv(const PanelView& P, const double* val64, const double* x, double* y,
+                 int mode, KrylovScalars* ks, double* partial, unsigned* counter,
+                 cudaStream_t s) {
   const int grid = kRedBlocks;
   switch (mode) {
     case 0: k_spmv<double, 0><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
@@ -623,10 +870,10 @@ cudaError_t pcg_init(int n, const double* b, const double* m, KrylovVecs& V,
   return cudaGetLastError();
 }
 
-cudaError_t pcg_iteration(const PanelView& P, const double* val64, const float* val32,
-                          int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
-                          double* partial, unsigned* counter, cudaStream_t s) {
-  cudaError_t e = spmv(P, val64, val32, V.p, V.q, 1, ks, partial, counter, s);
+cudaError_t pcg_iteration(const PanelView& P, const double* val64, int n, const double* m,
+                          KrylovVecs& V, KrylovScalars* ks, double* partial,
+                          unsigned* counter, cudaStream_t s) {
+  cudaError_t e = spmv(P, val64, V.p, V.q, 1, ks, partial, counter, s);
   if (e != cudaSuccess) return e;
   k_pcg_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, m, V.z, ks, partial,
                                             counter);
@@ -640,29 +887,30 @@ cudaError_t minres_conv(int n, const double* b, const double* m, KrylovScalars* 
   return cudaGetLastError();
 }
 
-cudaError_t minres_start(const PanelView& P, const double* val64, const float* val32,
-                         int n, const double* b, const double* m, KrylovVecs& V,
+cudaError_t minres_start(const PanelView& P, const double* val64, int n, const double* b,
+                         const double* m, KrylovVecs& V, const KrylovVecs32* pair,
                          KrylovScalars* ks, int maxit, bool zero_x, double* partial,
                          unsigned* counter, cudaStream_t s) {
   if (zero_x) {
     cudaMemsetAsync(V.x, 0, sizeof(double) * n, s);
     cudaMemsetAsync(V.q, 0, sizeof(double) * n, s);
   } else {
-    cudaError_t e = spmv(P, val64, val32, V.x, V.q, 0, ks, partial, counter, s);
+    cudaError_t e = spmv(P, val64, V.x, V.q, 0, ks, partial, counter, s);
     if (e != cudaSuccess) return e;
   }
   k_minres_start<<<vec_grid(n), 256, 0, s>>>(n, b, V.q, m, V.v, V.v0, V.w0, V.w00, V.z0,
-                                              ks, maxit, partial, counter);
+                                              ks, maxit, partial, counter,
+                                              pair ? pair->c : nullptr);
   return cudaGetLastError();
 }
 
-cudaError_t minres_iteration(const PanelView& P, const double* val64, const float* val32,
-                             int n, const double* m, KrylovVecs& V, KrylovScalars* ks,
-                             double* partial, unsigned* counter, cudaStream_t s) {
-  cudaError_t e = spmv(P, val64, val32, V.z0, V.p, 2, ks, partial, counter, s);
+cudaError_t minres_iteration(const PanelView& P, const double* val64, int n, const double* m,
+                             KrylovVecs& V, KrylovScalars* ks, double* partial,
+                             unsigned* counter, cudaStream_t s) {
+  cudaError_t e = spmv(P, val64, V.z0, V.p, 2, ks, partial, counter, s);
   if (e != cudaSuccess) return e;
   k_minres_lanczos<<<vec_grid(n), 256, 0, s>>>(n, V.p, V.v, V.v0, m, V.z, ks, partial,
-                                                counter);
+                                                counter, nullptr);
   k_minres_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.z0, V.w0, V.w00, V.v0, V.v, V.p,
                                                V.z, ks);
   return cudaGetLastError();
@@ -718,6 +966,106 @@ cudaError_t to_f32(int64_t n, const double* a, float* b, cudaStream_t s) {
   int64_t g = (n + 255) / 256;
   if (g > 8 * kRedBlocks) g = 8 * kRedBlocks;
   k_to_f32<<<(int)g, 256, 0, s>>>(n, a, b);
+  return cudaGetLastError();
+}
+
+// ---- compensated operator launchers ------------------------------------------
+cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s) {
+  int64_t g = (n + 255) / 256;
+  if (g > 8 * kRedBlocks) g = 8 * kRedBlocks;
+  if (g < 1) g = 1;
+  k_split_values<<<(int)g, 256, 0, s>>>(n, v, hi, lo);
+  return cudaGetLastError();
+}
+
+cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s) {
+  k_split_pair<<<vec_grid(n), 256, 0, s>>>(n, v, pr);
+  return cudaGetLastError();
+}
+
+// One wave: the SMs times the CTAs of this variant resident per SM (at
+// most kRedBlocks, the size of the reduction partials), so no CTA waits for
+// a second, partly filled wave.
+template <typename K>
+int resident_grid(K kernel) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess ||
+      per_sm < 1)
+    return kRedBlocks;
+  const int g = sms * per_sm;
+  return g < kRedBlocks ? g : kRedBlocks;
+}
+
+template <int MODE, int S, int U>
+void launch_cf(const PanelView& P, CompVals C, const float2* xp, double* y, const double* xd,
+               KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s) {
+  static const int grid = resident_grid(k_spmv_cf<MODE, S, U>);
+  k_spmv_cf<MODE, S, U><<<grid, 256, 0, s>>>(
+      P, C.hi, C.lo, xp, y, xd, ks, partial, counter);
+}
+
+// C.shape = 10 * lanes-per-node code (0: 8, 1: 16, 2: 32) + columns per trip
+template <int MODE>
+void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
+                    const double* xd, KrylovScalars* ks, double* partial, unsigned* counter,
+                    cudaStream_t s) {
+  switch (C.shape) {
+    case 2: launch_cf<MODE, 8, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 4: launch_cf<MODE, 8, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 11: launch_cf<MODE, 16, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 12: launch_cf<MODE, 16, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 14: launch_cf<MODE, 16, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 21: launch_cf<MODE, 32, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 22: launch_cf<MODE, 32, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 24: launch_cf<MODE, 32, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    default: launch_cf<MODE, 8, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
+  }
+}
+
+cudaError_t spmvc(const PanelView& P, CompVals C, const float2* xp, double* y, cudaStream_t s) {
+  launch_spmv_cf<0>(P, C, xp, y, nullptr, nullptr, nullptr, nullptr, s);
+  return cudaGetLastError();
+}
+
+cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,
+                      KrylovVecs32& V32, KrylovScalars* ks, double tol, double conv_abs,
+                      int maxit, double* partial, unsigned* counter, cudaStream_t s) {
+  k_pcgc_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.r, V.z, V.p, V32.c, V.x, ks, tol,
+                                           conv_abs, maxit, partial, counter);
+  return cudaGetLastError();
+}
+
+cudaError_t pcgc_iteration(const PanelView& P, CompVals C, int n, const double* m,
+                           KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                           double* partial, unsigned* counter, cudaStream_t s) {
+  launch_spmv_cf<1>(P, C, V32.c, V.q, V.p, ks, partial, counter, s);
+  k_pcg_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, m, V.z, ks, partial,
+                                            counter);
+  k_pcgc_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, V32.c, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const double* m,
+                              KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                              double* partial, unsigned* counter, cudaStream_t s) {
+  launch_spmv_cf<2>(P, C, V32.c, V.p, V.z0, ks, partial, counter, s);
+  k_minres_lanczos<<<vec_grid(n), 256, 0, s>>>(n, V.p, V.v, V.v0, m, V.z, ks, partial,
+                                                counter, V32.c);
+  k_minres_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.z0, V.w0, V.w00, V.v0, V.v, V.p,
+                                               V.z, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t true_residual(int n, const double* b, const double* q, const double* m, int absval,
+                          double* r, double* out, double* partial, unsigned* counter,
+                          cudaStream_t s) {
+  k_true_residual<<<vec_grid(n), 256, 0, s>>>(n, b, q, m, absval, r, out, partial, counter);
   return cudaGetLastError();
 }
 

@@ -219,6 +219,75 @@ def test_mixed_precision_refinement():
         assert np.abs(u[:, sl] - v[:, sl]).max() <= 1e-8 * np.abs(u[:, sl]).max()
 
 
+def _abs_product(m, x):
+    """(|A| |x|) from the host CSRD copy: the scale of the rounding bound."""
+    import scipy.sparse as sp
+    ia, ja, ad, al = m.get_csrd()
+    L = sp.csr_matrix((np.abs(al), ja - 1, ia - 1), shape=(m.neq, m.neq))
+    ax = np.abs(x)
+    return np.abs(ad) * ax + L @ ax + L.T @ ax
+
+
+def test_compensated_spmv_rounding_bound(problems):
+    """PM_FP32C_REFINE operator: values FP32 + an int8 relative correction
+    (within 2^-32 |v|), x as an FP32 pair (2^-48), compensated sums: each row
+    is within 2^-30 (|A| |x|)_i of the FP64 product."""
+    rng = np.random.default_rng(6)
+    for pb in problems:
+        m = pg.from_problem(pb)
+        m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+        x = rng.standard_normal(m.neq)
+        y64 = m.matvec(x)
+        m.set_precision(pg.capi.PM_FP32C_REFINE)
+        yc = m.matvec(x)
+        bound = 2.0 ** -30 * _abs_product(m, x) + 1e-300
+        assert np.all(np.abs(yc - y64) <= bound), np.max(np.abs(yc - y64) / bound)
+        assert not np.array_equal(yc, y64)  # the compensated path did run
+
+
+@pytest.mark.parametrize("solver,precond,cases", [(1, 2, [2, 4]), (7, 5, [1, 3])])
+def test_compensated_solve_matches_fp64(problems, solver, precond, cases):
+    """The compensated operator inside the FP64 refinement reaches the FP64
+    solution: same stopping test, FP64 outer residual."""
+    for k in cases:
+        pb = problems[k]
+        m = pg.from_problem(pb)
+        m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+        b = np.random.default_rng(7).standard_normal(m.neq)
+        tol = 1e-11
+        x64, _ = m.solve(b, solver=solver, precond=precond, tol=tol, maxit=400000)
+        m.set_precision(pg.capi.PM_FP32C_REFINE)
+        xc, info = m.solve(b, solver=solver, precond=precond, tol=tol, maxit=400000)
+        assert info.refine >= 1
+        assert np.abs(xc - x64).max() <= 1e4 * tol * np.abs(x64).max()
+        # the FP64 residual of the result meets the solver's own test:
+        # sqrt|(r, m r)| < tol sqrt|(b, m b)|, m = 1/ad (PCG) or |1/ad| (MINRES)
+        m.set_precision(pg.capi.PM_FP64)  # matvec follows the precision mode
+        r = b - m.matvec(xc)
+        _, _, ad, _ = m.get_csrd()
+        w = 1.0 / ad if precond == 2 else np.abs(1.0 / ad)
+        rn = np.sqrt(abs(np.sum(r * r * w)))
+        bn = np.sqrt(abs(np.sum(b * b * w)))
+        assert rn <= 1.01 * tol * bn, (rn, tol * bn)
+
+
+def test_compensated_steps_match_fp64():
+    """Three steps of the heterogeneous cube in PM_FP32C_REFINE stay within
+    1e-8 relative of the FP64 steps at the same tolerance."""
+    pb = meshgen.cube_problem(n=6)
+    m64 = pg.from_problem(pb)
+    mc = pg.from_problem(pb)
+    mc.set_precision(pg.capi.PM_FP32C_REFINE)
+    for k in range(3):
+        a = m64.step(maxnlit=2, stop_crit=1, solvtol=1e-10)
+        c = mc.step(maxnlit=2, stop_crit=1, solvtol=1e-10)
+        assert c.refine >= 1 and c.nlit == a.nlit
+    u, _, _ = m64.get_state()
+    v, _, _ = mc.get_state()
+    for sl in (slice(0, 3), slice(3, 4)):
+        assert np.abs(u[:, sl] - v[:, sl]).max() <= 1e-8 * np.abs(u[:, sl]).max()
+
+
 def test_errors_are_returned_not_fatal(problems):
     # maxit exceeded -> status 4, and the handle stays usable
     pb = problems[2]
