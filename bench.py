@@ -58,7 +58,8 @@ def parse():
     ap.add_argument("--spmv-only", action="store_true",
                     help="time the SpMV alone on the assembled cube of --n")
     ap.add_argument("--reps", type=int, default=20)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"],
+                    help="operator of --spmv-only and --profile")
     return ap.parse_args()
 
 
@@ -286,6 +287,8 @@ def run_gpu(args):
     step_kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=args.solvtol,
                    maxit=200000, reassemble=True)
     if args.profile:
+        if args.precision == "fp32c":
+            m.set_precision(pg.capi.PM_FP32C_REFINE)
         info = m.step(**step_kw)
         torch.cuda.synchronize()
         print(json.dumps({"profile_step": True, "pcg_iterations": info.iters,

@@ -304,7 +304,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   pm::KrylovVecs32& V32 = h->D.kv32;
   const pm::PanelView P = h->P.view();
   const double* val64 = h->P.val;
-  const pm::CompVals C{h->P.valh, h->P.vall, h->shape};
+  const pm::CompVals C = h->P.comp(h->shape);
   pm::KrylovScalars ks{};
   int sweeps = 0;
   cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
@@ -547,7 +547,7 @@ int solve_mixed(Handle* h, int solver, const double* d_b, double* d_x, double to
 }
 
 // Autotuner of the compensated SpMV: times each shape (lanes per node 8, 16,
-// 32 x columns per lane and trip 1, 2, 4) on this matrix, 3 launches each
+// 32 x columns per lane and trip 1, 2, 4, and the record kernel) on this matrix, 3 launches each
 // after one warm-up, with CUDA events on the launching stream, and keeps the
 // fastest for the handle's lifetime (graphs captured later bake it in).
 // PM_SPMV_SHAPE=<code> in the environment fixes the choice instead.
@@ -556,7 +556,7 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   if (const char* env = std::getenv("PM_SPMV_SHAPE")) {
     const int u = std::atoi(env);
     for (int c : pm::kCfShapes)
-      if (u == c) {
+      if (u == c && !(c == pm::kCaShape && h->P.ca_warps == 0)) {
         h->shape = u;
         return PM_OK;
       }
@@ -566,7 +566,8 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   float best = 0.f;
   int best_c = 1;
   for (int c : pm::kCfShapes) {
-    const pm::CompVals C{h->P.valh, h->P.vall, c};
+    if (c == pm::kCaShape && h->P.ca_warps == 0) continue;  // records do not fit in smem
+    const pm::CompVals C = h->P.comp(c);
     PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
     PM_CUDA(cudaEventRecord(h->ev[0], s));
     for (int k = 0; k < 3; ++k) PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
@@ -586,14 +587,23 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
 }
 
 // Compensated copies of the current FP64 panel values (PM_FP32C_REFINE).
+// Until the autotuner has chosen, both layouts are written; afterwards only
+// the one its shape reads.
 int ensure_comp(Handle* h, cudaStream_t s) {
   if (h->assembledC) return PM_OK;
   if (!h->P.valh) {
     PM_CUDA(cudaMalloc(&h->P.valh, sizeof(float) * (size_t)h->P.nnz));
     PM_CUDA(cudaMalloc(&h->P.vall, sizeof(int8_t) * (size_t)h->P.nnz));
+    PM_TRY(pm::build_rec_layout(h));
   }
-  h->launches += 1;
-  PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
+  if (h->shape != pm::kCaShape) {
+    h->launches += 1;
+    PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
+  }
+  if (h->shape == 0 || h->shape == pm::kCaShape) {
+    h->launches += 1;
+    PM_CUDA(pm::split_records(h->P.view(), h->P.val, h->P.comp(h->shape), s));
+  }
   h->assembledC = true;
   return tune_spmvc(h, s);
 }
@@ -605,7 +615,7 @@ int spmv_op(Handle* h, const double* d_x, double* d_y, cudaStream_t s) {
     PM_TRY(ensure_comp(h, s));
     h->launches += 2;
     PM_CUDA(pm::split_pair(h->neq, d_x, h->D.kv32.c, s));
-    PM_CUDA(pm::spmvc(h->P.view(), pm::CompVals{h->P.valh, h->P.vall, h->shape}, h->D.kv32.c,
+    PM_CUDA(pm::spmvc(h->P.view(), h->P.comp(h->shape), h->D.kv32.c,
                       d_y, s));
     return PM_OK;
   }
@@ -702,7 +712,8 @@ void free_all(Handle* h) {
                   D.ad, D.m, D.bx, D.by, D.rr, D.dx, D.xs, D.kv.x, D.kv.r, D.kv.z, D.kv.p, D.kv.q,
                   D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
-                  P.val32, P.valh, P.vall, P.node_val_off, P.node_W, P.order};
+                  P.val32, P.valh, P.vall, P.rec, P.rec_off, P.node_val_off, P.node_W,
+                  P.order};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})

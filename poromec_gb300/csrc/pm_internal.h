@@ -48,11 +48,18 @@ struct Panels {
   float* val32 = nullptr;  // FP32 values (PM_FP32_REFINE)
   float* valh = nullptr;      // compensated values (PM_FP32C_REFINE): fl32(v)
   int8_t* vall = nullptr;     //   and round((v - fl32(v)) / fl32(v) * 2^31)
+  // the same values as node records for the record kernel (CompVals)
+  uint8_t* rec = nullptr;
+  int64_t* rec_off = nullptr;
+  int rec_max = 0, ca_warps = 0, ca_grid = 0;
   // indexed by node id - 1
   int64_t* node_val_off = nullptr;
   int32_t* node_W = nullptr;
   PanelView view() const {
     return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols};
+  }
+  CompVals comp(int shape) const {
+    return CompVals{valh, vall, rec, rec_off, rec_max, ca_warps, ca_grid, shape};
   }
 };
 
@@ -132,6 +139,7 @@ struct Handle {
   std::vector<int32_t> h_ie;
   // host copies of the panel structure (pm_get_csrd)
   std::vector<int32_t> h_eq0, h_d, h_W, h_low, h_cols;
+  std::vector<int32_t> h_order;    // SpMV visiting order of the active nodes
   std::vector<int64_t> h_val_off, h_col_off;
   int nloads = 0, maxt = 1;
   double gravity[3] = {0.0, 0.0, -9.81};
@@ -161,5 +169,6 @@ struct Handle {
 // pm_setup.cpp
 int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
                     const int32_t* fnno, const double* x, const int32_t* num);
+int build_rec_layout(Handle* h);
 
 }  // namespace pm

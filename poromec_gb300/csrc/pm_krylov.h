@@ -96,11 +96,27 @@ cudaError_t to_f32(int64_t n, const double* a, float* b, cudaStream_t s);
 struct CompVals {
   const float* hi;
   const int8_t* lo;
+  // Record layout (shape kCaShape): per active node one 16-byte aligned record
+  // at rec + rec_off[node]: d rows of Wp = W rounded up to 4 FP32 hi values,
+  // then d * Wp biased corrections qb = q + 128 (padded to 16 bytes), then
+  // the Wp column indices (pad columns repeat the last one, with zero values).
+  // Records follow the SpMV visiting order, so the product streams them.
+  const uint8_t* rec;
+  const int64_t* rec_off;
+  int rec_max;   // bytes of the largest record
+  int ca_warps;  // warps per CTA of the record kernel (two records each in smem)
+  int ca_grid;   // its CTAs (resident on all SMs)
   int shape;  // SpMV shape: 10 * (0: 8, 1: 16, 2: 32 lanes per node) + columns
-              // per lane and trip (1, 2, 4)
+              // per lane and trip (1, 2, 4); kCaShape: the record kernel
 };
-constexpr int kCfShapes[] = {1, 2, 4, 11, 12, 14, 21, 22, 24};
+constexpr int kCaShape = 90;
+constexpr int kCfShapes[] = {1, 2, 4, 11, 12, 14, 21, 22, 24, kCaShape};
 cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
+cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s);
+// Dynamic shared memory of the record kernel for a given record size and
+// warp count, and the set-up of its launch attributes (once per process).
+int ca_smem_bytes(int rec_max, int warps);
+cudaError_t ca_configure(int rec_max, int* warps, int* grid);
 cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s);
 cudaError_t spmvc(const PanelView& P, CompVals C, const float2* xp, double* y, cudaStream_t s);
 cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,

@@ -254,6 +254,7 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
   P.nnz = vo;
   P.ncols = co;
   int st;
+  h->h_order = order;
   if ((st = upload(h, &P.order, order.data(), nact))) return st;
   if ((st = upload(h, &P.eq0, h->h_eq0.data(), nact))) return st;
   if ((st = upload(h, &P.d, h->h_d.data(), nact))) return st;
@@ -273,6 +274,34 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
   if ((st = upload(h, &h->D.dofkind, kind.data(), kind.size()))) return st;
   if ((st = upload(h, &h->D.fnno, fnno, (size_t)nnode))) return st;
   h->h_fnno.assign(fnno, fnno + nnode);
+  return PM_OK;
+}
+
+// Offsets of the node records of the compensated operator (layout in
+// CompVals): 16-byte aligned, in the SpMV visiting order; the records
+// themselves are written on the device from the FP64 panels.
+int build_rec_layout(Handle* h) {
+  Panels& P = h->P;
+  const int nact = P.nact;
+  std::vector<int64_t> off(nact > 0 ? nact : 1, 0);
+  int64_t o = 0;
+  int rmax = 16;
+  for (int i = 0; i < nact; ++i) {
+    const int k = h->h_order[i];
+    const int d = h->h_d[k], Wp = (h->h_W[k] + 3) & ~3;
+    const int R = 4 * d * Wp + ((d * Wp + 15) & ~15) + 4 * Wp;
+    off[k] = o;
+    o += R;
+    if (R > rmax) rmax = R;
+  }
+  int st;
+  if ((st = upload(h, &P.rec_off, off.data(), off.size()))) return st;
+  if ((st = upload<uint8_t>(h, &P.rec, nullptr, (size_t)(o > 0 ? o : 16)))) return st;
+  P.rec_max = rmax;
+  if (ca_configure(rmax, &P.ca_warps, &P.ca_grid) != cudaSuccess) {
+    h->err = "record SpMV set-up failed";
+    return PM_E_CUDA;
+  }
   return PM_OK;
 }
 

@@ -651,6 +651,217 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---- record kernel: node records streamed into shared memory by cp.async ----
+// Each warp takes nodes gw, gw + nw, ... of the visiting order (gw its global
+// warp index, nw the warps of the grid) and keeps two record buffers in
+// shared memory: while it computes node i from one, the 16-byte cp.async
+// copies of node i + nw stream into the other.  The bytes in flight per SM
+// are then set by the buffers (about a record per warp), not by the loads a
+// thread holds in registers, which bounds the register kernels above at
+// the read bandwidth of one 16-byte load per thread in flight.  The copies
+// complete through cp.async.wait_group, so the kernel contains no
+// spin-wait of its own.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// (qb_k - 128) * 2^-31 for byte k of a packed word of biased corrections,
+// exactly: the byte permute builds the float 1.5 * 2^23 + qb_k; scaling by
+// 2^-31 and removing (1.5 * 2^23 + 128) * 2^-31 = 0x1.8001p-8 is exact.
+__device__ __forceinline__ float qb_scale(unsigned w, int k) {
+  const float f = __int_as_float((int)__byte_perm(w, 0x4B400000u, 0x7640u | (unsigned)k));
+  return fmaf(f, 0x1p-31f, -0x1.8001p-8f);
+}
+
+__device__ __forceinline__ void f2_fma_s(F2& acc, float vh, float qs, float xh, float xl) {
+  const float t = vh * xh;
+  const float e = fmaf(vh, xh, -t);
+  const float c = fmaf(vh, xl, fmaf(t, qs, e));
+  two_sum_acc(acc, t);
+  acc.c += c;
+}
+
+__device__ __forceinline__ int rec_bytes(int d, int Wp) {
+  return 4 * d * Wp + ((d * Wp + 15) & ~15) + 4 * Wp;
+}
+
+// Rows of one node from its record in shared memory: lane t takes column
+// quads t, t + 32, t + 64 per trip, issues the 12 gathers of x pairs for
+// them, then the compensated products of the d rows.
+template <int D>
+__device__ __forceinline__ void ca_rows(const float4* __restrict__ h4,
+                                        const unsigned* __restrict__ q4,
+                                        const int4* __restrict__ c4,
+                                        const float2* __restrict__ xp, int nq, int lane,
+                                        F2 (&a)[4]) {
+  for (int j0 = lane; j0 < nq; j0 += 96) {
+    float2 xv[3][4];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int j = j0 + 32 * u;
+      const int4 cc = j < nq ? c4[j] : make_int4(0, 0, 0, 0);
+      xv[u][0] = xp[cc.x];
+      xv[u][1] = xp[cc.y];
+      xv[u][2] = xp[cc.z];
+      xv[u][3] = xp[cc.w];
+    }
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int j = j0 + 32 * u;
+      if (j < nq) {
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          const float4 hv = h4[r * nq + j];
+          const unsigned qv = q4[r * nq + j];
+          f2_fma_s(a[r], hv.x, qb_scale(qv, 0), xv[u][0].x, xv[u][0].y);
+          f2_fma_s(a[r], hv.y, qb_scale(qv, 1), xv[u][1].x, xv[u][1].y);
+          f2_fma_s(a[r], hv.z, qb_scale(qv, 2), xv[u][2].x, xv[u][2].y);
+          f2_fma_s(a[r], hv.w, qb_scale(qv, 3), xv[u][3].x, xv[u][3].y);
+        }
+      }
+    }
+  }
+}
+
+// MODE as k_spmv_cf.  Shared memory: per warp two buffers of C.rec_max
+// bytes, then per warp 32 staged row results (float2) and their equations.
+// Row results leave the butterfly in 4 lanes; they are staged and converted
+// to FP64 (and dotted with xd) 32 at a time, so the FP64 instructions, which
+// cost a full warp's pipe time whatever their mask, run with all lanes on.
+template <int MODE>
+__global__ void __launch_bounds__(512, 1)
+    k_spmv_ca(PanelView P, CompVals C, const float2* __restrict__ xp, double* __restrict__ y,
+              const double* __restrict__ xd, KrylovScalars* ks, double* partial,
+              unsigned* counter) {
+  if (MODE != 0)
+    if (krylov_skip(ks, true)) return;
+  extern __shared__ __align__(16) unsigned char ca_smem[];
+  const int lane = threadIdx.x & 31, w = (int)(threadIdx.x >> 5);
+  const int nwb = (int)(blockDim.x >> 5);
+  const size_t rmax = (size_t)C.rec_max;
+  unsigned char* buf = ca_smem + (size_t)w * 2 * rmax;
+  float2* o_sc = reinterpret_cast<float2*>(ca_smem + (size_t)nwb * 2 * rmax) + w * 32;
+  int* o_eq = reinterpret_cast<int*>(ca_smem + (size_t)nwb * 2 * rmax +
+                                     (size_t)nwb * 32 * sizeof(float2)) + w * 32;
+  const int gw = (int)blockIdx.x * nwb + w, nw = (int)gridDim.x * nwb;
+  auto issue = [&](int i, int b) {
+    const int k = P.order[i];
+    const int R = rec_bytes(P.d[k], (P.W[k] + 3) & ~3);
+    const unsigned char* src = C.rec + C.rec_off[k];
+    unsigned char* dst = buf + (size_t)b * rmax;
+    for (int c = lane * 16; c < R; c += 32 * 16) cp_async16(dst + c, src + c);
+  };
+  double dsum = 0.0;
+  int count = 0;  // staged rows of this warp (warp-uniform)
+  auto flush = [&]() {
+    __syncwarp();
+    if (lane < count) {
+      const float2 sc = o_sc[lane];
+      const int e = o_eq[lane];
+      const double v = double(sc.x) + double(sc.y);
+      y[e] = v;
+      if (MODE != 0) dsum += v * xd[e];
+    }
+    __syncwarp();
+    count = 0;
+  };
+  if (gw < P.nact) issue(gw, 0);
+  cp_async_commit();
+  int it = 0;
+  for (int i = gw; i < P.nact; i += nw, ++it) {
+    if (i + nw < P.nact) issue(i + nw, (it + 1) & 1);
+    cp_async_commit();
+    cp_async_wait<1>();  // this lane's copies of node i have landed
+    __syncwarp();        // ... and every other lane's
+    const int k = P.order[i];
+    const int d = P.d[k], e0 = P.eq0[k];
+    const int Wp = (P.W[k] + 3) & ~3, nq = Wp >> 2;
+    const unsigned char* b = buf + (size_t)(it & 1) * rmax;
+    const float4* h4 = reinterpret_cast<const float4*>(b);
+    const unsigned* q4 = reinterpret_cast<const unsigned*>(b + 4 * d * Wp);
+    const int4* c4 = reinterpret_cast<const int4*>(b + 4 * d * Wp + ((d * Wp + 15) & ~15));
+    F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    if (d == 4) ca_rows<4>(h4, q4, c4, xp, nq, lane, a);
+    else if (d == 3) ca_rows<3>(h4, q4, c4, xp, nq, lane, a);
+    else if (d == 2) ca_rows<2>(h4, q4, c4, xp, nq, lane, a);
+    else ca_rows<1>(h4, q4, c4, xp, nq, lane, a);
+    __syncwarp();  // the buffer is read; the next trip refills it
+    // transposed butterfly over the 32 lanes (as in k_spmv_cf)
+    const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
+    F2 k0 = h1 ? a[2] : a[0], k1 = h1 ? a[3] : a[1];
+    k0 = f2_add(k0, f2_shfl(h1 ? a[0] : a[2], 16));
+    k1 = f2_add(k1, f2_shfl(h1 ? a[1] : a[3], 16));
+    F2 kk = h2 ? k1 : k0;
+    kk = f2_add(kk, f2_shfl(h2 ? k0 : k1, 8));
+    kk = f2_add(kk, f2_shfl(kk, 4));
+    kk = f2_add(kk, f2_shfl(kk, 2));
+    kk = f2_add(kk, f2_shfl(kk, 1));
+    const int r = (h1 ? 2 : 0) + (h2 ? 1 : 0);
+    if (count + d > 32) flush();
+    if ((lane & 7) == 0 && r < d) {
+      o_sc[count + r] = make_float2(kk.s, kk.c);
+      o_eq[count + r] = e0 + r;
+    }
+    count += d;
+  }
+  cp_async_wait<0>();
+  flush();
+  if (MODE != 0) {
+    double in[1] = {dsum}, tot[1];
+    if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+      if (MODE == 1) {
+        ks->pq = tot[0];
+        ks->alpha = ks->d / tot[0];
+      } else {
+        ks->alpha = fabs(tot[0]) * (1.0 / (ks->beta * ks->beta));
+      }
+    }
+  }
+}
+
+// FP64 panel values (rows of W) -> node records (layout in CompVals): one
+// warp per node, coalesced on both sides.  hi = fl32(v), qb = 128 +
+// round((v - hi) / hi * 2^31) clamped to [1, 255]; pad columns get hi = 0,
+// qb = 128 and repeat the last column index.
+__global__ void __launch_bounds__(256)
+    k_split_records(PanelView P, const double* __restrict__ val, uint8_t* __restrict__ rec,
+                    const int64_t* __restrict__ rec_off) {
+  const int lane = threadIdx.x & 31;
+  const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
+  for (int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); k < P.nact; k += nwarp) {
+    const int d = P.d[k], W = P.W[k], Wp = (W + 3) & ~3;
+    const double* v = val + P.val_off[k];
+    uint8_t* base = rec + rec_off[k];
+    float* hi = reinterpret_cast<float*>(base);
+    uint8_t* qb = base + 4 * d * Wp;
+    const int qpad = (d * Wp + 15) & ~15;
+    int32_t* cols = reinterpret_cast<int32_t*>(base + 4 * d * Wp + qpad);
+    for (int r = 0; r < d; ++r)
+      for (int c = lane; c < Wp; c += 32) {
+        float h = 0.f, q = 0.f;
+        if (c < W) {
+          const double a = v[(size_t)r * W + c];
+          h = float(a);
+          // a - h is exact in FP64; the quotient in FP32 moves q by < 1e-5
+          if (h != 0.f && isfinite(h)) q = rintf(float(a - double(h)) / h * 2147483648.0f);
+        }
+        hi[r * Wp + c] = h;
+        qb[r * Wp + c] = (uint8_t)(128 + (int)fminf(fmaxf(q, -127.f), 127.f));
+      }
+    for (int c = d * Wp + lane; c < qpad; c += 32) qb[c] = 128;
+    const int32_t* src = P.cols + P.col_off[k];
+    for (int c = lane; c < Wp; c += 32) cols[c] = src[c < W ? c : W - 1];
+  }
+}
+
 // FP64 panel values -> (hi = fl32(v), q = round((v - hi) / hi * 2^31)),
 // |q| clamped to 127 (a tie at the rounding bound costs one unit, 2^-31).
 __global__ void k_split_values(int64_t n, const double* __restrict__ v, float* __restrict__ hi,
@@ -660,9 +871,12 @@ __global__ void k_split_values(int64_t n, const double* __restrict__ v, float* _
     const double a = v[i];
     const float h = float(a);
     hi[i] = h;
-    double q = 0.0;
-    if (h != 0.f && isfinite(h)) q = rint((a - double(h)) / double(h) * 2147483648.0);
-    lo[i] = (int8_t)fmin(fmax(q, -127.0), 127.0);
+    // a - h is exact in FP64; the quotient is formed in FP32 (its 2^-24
+    // relative error moves q by less than 1e-5), which keeps the FP64 pipe,
+    // 1/64 of the FP32 rate on this part, to two operations per value
+    float q = 0.f;
+    if (h != 0.f && isfinite(h)) q = rintf(float(a - double(h)) / h * 2147483648.0f);
+    lo[i] = (int8_t)fminf(fmaxf(q, -127.f), 127.f);
   }
 }
 
@@ -978,6 +1192,11 @@ cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cuda
   return cudaGetLastError();
 }
 
+cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s) {
+  k_split_records<<<8 * kRedBlocks, 256, 0, s>>>(P, v, const_cast<uint8_t*>(C.rec), C.rec_off);
+  return cudaGetLastError();
+}
+
 cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s) {
   k_split_pair<<<vec_grid(n), 256, 0, s>>>(n, v, pr);
   return cudaGetLastError();
@@ -1010,12 +1229,49 @@ void launch_cf(const PanelView& P, CompVals C, const float2* xp, double* y, cons
       P, C.hi, C.lo, xp, y, xd, ks, partial, counter);
 }
 
-// C.shape = 10 * lanes-per-node code (0: 8, 1: 16, 2: 32) + columns per trip
+int ca_smem_bytes(int rec_max, int warps) {
+  return warps * (2 * rec_max + 32 * (int)(sizeof(float2) + sizeof(int)));
+}
+
+// Warps per CTA of the record kernel: as many as the opt-in shared memory
+// holds two records each for, at most 16; grid: the CTAs resident on all SMs.
+cudaError_t ca_configure(int rec_max, int* warps, int* grid) {
+  int dev = 0, smem = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  int wn = 16;
+  while (wn > 0 && ca_smem_bytes(rec_max, wn) > smem) --wn;
+  *warps = wn;
+  *grid = 0;
+  if (wn == 0) return cudaSuccess;
+  const int bytes = ca_smem_bytes(rec_max, wn);
+  e = cudaFuncSetAttribute(k_spmv_ca<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_spmv_ca<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_spmv_ca<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv_ca<1>, wn * 32, bytes);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  *grid = sms * per_sm < kRedBlocks ? sms * per_sm : kRedBlocks;
+  return cudaSuccess;
+}
+
+// C.shape = 10 * lanes-per-node code (0: 8, 1: 16, 2: 32) + columns per trip,
+// or kCaShape for the record kernel
 template <int MODE>
 void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
                     const double* xd, KrylovScalars* ks, double* partial, unsigned* counter,
                     cudaStream_t s) {
   switch (C.shape) {
+    case kCaShape:
+      k_spmv_ca<MODE><<<C.ca_grid, C.ca_warps * 32, ca_smem_bytes(C.rec_max, C.ca_warps), s>>>(
+          P, C, xp, y, xd, ks, partial, counter);
+      break;
     case 2: launch_cf<MODE, 8, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 4: launch_cf<MODE, 8, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 11: launch_cf<MODE, 16, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;

@@ -228,10 +228,13 @@ def _abs_product(m, x):
     return np.abs(ad) * ax + L @ ax + L.T @ ax
 
 
-def test_compensated_spmv_rounding_bound(problems):
+@pytest.mark.parametrize("shape", [None, 1, 14, 24, 90])
+def test_compensated_spmv_rounding_bound(problems, shape, monkeypatch):
     """PM_FP32C_REFINE operator: values FP32 + an int8 relative correction
     (within 2^-32 |v|), x as an FP32 pair (2^-48), compensated sums: each row
     is within 2^-30 (|A| |x|)_i of the FP64 product."""
+    if shape is not None:  # a fixed kernel shape instead of the autotuner's choice
+        monkeypatch.setenv("PM_SPMV_SHAPE", str(shape))
     rng = np.random.default_rng(6)
     for pb in problems:
         m = pg.from_problem(pb)
@@ -243,6 +246,8 @@ def test_compensated_spmv_rounding_bound(problems):
         bound = 2.0 ** -30 * _abs_product(m, x) + 1e-300
         assert np.all(np.abs(yc - y64) <= bound), np.max(np.abs(yc - y64) / bound)
         assert not np.array_equal(yc, y64)  # the compensated path did run
+        if shape is not None:
+            assert m.tune_spmv() == shape
 
 
 @pytest.mark.parametrize("solver,precond,cases", [(1, 2, [2, 4]), (7, 5, [1, 3])])
