@@ -79,6 +79,25 @@ int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
                    const int32_t* fnno, const double* x, int numat,
                    const int32_t* ie, const double* e, const int32_t* num,
                    pm_handle* out);
+
+/* A batch of independent meshes in one handle (the reference runs one mesh
+ * per process; this has no single counterpart there).  The arrays are those
+ * of pm_mesh_create for the union of the meshes, node ids and element
+ * connectivities offset so that instance i owns nodes
+ * inst_node_ptr[i] .. inst_node_ptr[i+1]-1 (0-based, inst_node_ptr[0] = 0,
+ * inst_node_ptr[ninst] = nnode) and each element lies inside one instance.
+ * pm_solve and pm_step then solve every instance independently, as if each
+ * were its own handle (own PCG scalars, stopping test, nonlinear test), in
+ * shared launches: PCG (solver 1) only, in PM_FP64 or PM_FP32C_REFINE. */
+int pm_batch_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
+                    const int32_t* ix, const int32_t* id, const int32_t* fnno,
+                    const double* x, int numat, const int32_t* ie, const double* e,
+                    int ninst, const int32_t* inst_node_ptr, pm_handle* h);
+
+/* Per instance of a batch: Krylov iterations of the last pm_solve or
+ * pm_step (summed over its nonlinear iterations) and the nonlinear iteration
+ * at which the last pm_step met its test; n >= ninst. */
+int pm_get_batch_iters(pm_handle h, int* iters, int* nlit, int n);
 void pm_destroy(pm_handle h);
 const char* pm_last_error(pm_handle h);
 const char* pm_status_string(int status);

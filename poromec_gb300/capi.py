@@ -64,6 +64,8 @@ def load(path=None):
     lib.pm_destroy.restype = None
     lib.pm_destroy.argtypes = [c_p]
     lib.pm_mesh_create.argtypes = [c_i] * 7 + [c_p] * 4 + [c_i] + [c_p] * 4
+    lib.pm_batch_create.argtypes = [c_i] * 7 + [c_p] * 4 + [c_i] + [c_p] * 2 + [c_i] + [c_p] * 2
+    lib.pm_get_batch_iters.argtypes = [c_p, c_p, c_p, c_i]
     lib.pm_set_loads.argtypes = [c_p] * 5 + [c_i, c_i, c_p, c_p]
     lib.pm_set_env.argtypes = [c_p, c_p, c_d, c_d, c_i]
     lib.pm_set_state.argtypes = [c_p] * 4
@@ -110,7 +112,8 @@ class Mesh:
     are 1-based as in the reference.
     """
 
-    def __init__(self, nnode, nnodev, numel, nen, nenv, ix, idflag, fnno, x, ie, e, num=None):
+    def __init__(self, nnode, nnodev, numel, nen, nenv, ix, idflag, fnno, x, ie, e, num=None,
+                 inst_node_ptr=None):
         self.lib = load()
         self.nnode, self.numel, self.nen, self.nenv = int(nnode), int(numel), int(nen), int(nenv)
         ix, idflag, fnno, ie, num = map(_i32, (ix, idflag, fnno, ie, num))
@@ -120,11 +123,22 @@ class Mesh:
         if e.shape[1] < PM_PROP:
             e = np.pad(e, ((0, 0), (0, PM_PROP - e.shape[1])))
         h = ctypes.c_void_p()
-        st = self.lib.pm_mesh_create(self.nnode, int(nnodev), self.numel, self.nen, self.nenv, 3,
-                                     4, _p(ix), _p(idflag), _p(fnno), _p(x), len(ie), _p(ie),
-                                     _p(e), _p(num), ctypes.byref(h))
+        self.ninst = 0
+        if inst_node_ptr is None:
+            st = self.lib.pm_mesh_create(self.nnode, int(nnodev), self.numel, self.nen,
+                                         self.nenv, 3, 4, _p(ix), _p(idflag), _p(fnno), _p(x),
+                                         len(ie), _p(ie), _p(e), _p(num), ctypes.byref(h))
+            what = "pm_mesh_create"
+        else:
+            ptr = _i32(inst_node_ptr)
+            self.ninst = len(ptr) - 1
+            st = self.lib.pm_batch_create(self.nnode, int(nnodev), self.numel, self.nen,
+                                          self.nenv, 3, 4, _p(ix), _p(idflag), _p(fnno), _p(x),
+                                          len(ie), _p(ie), _p(e), self.ninst, _p(ptr),
+                                          ctypes.byref(h))
+            what = "pm_batch_create"
         if st != 0:
-            raise PMError(st, "pm_mesh_create")
+            raise PMError(st, what)
         self.h = h
         neq, nad, nc, nnz = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()
         self.lib.pm_get_sizes(h, ctypes.byref(neq), ctypes.byref(nad), ctypes.byref(nc),
@@ -179,6 +193,15 @@ class Mesh:
 
     def set_refine(self, inner_tol=1e-5):
         self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
+
+    def batch_iters(self):
+        """Per instance of a batch: Krylov iterations of the last solve or
+        step and the nonlinear iteration at which the last step stopped."""
+        it = np.zeros(self.ninst, np.int32)
+        nl = np.zeros(self.ninst, np.int32)
+        self._check(self.lib.pm_get_batch_iters(self.h, _p(it), _p(nl), self.ninst),
+                    "pm_get_batch_iters")
+        return it, nl
 
     def tune_spmv(self):
         """Autotune the compensated SpMV on the assembled matrix; returns the
@@ -273,7 +296,7 @@ def from_problem(pb, num=None):
     state applied."""
     m = Mesh(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]), int(pb["nen"]),
              int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"],
-             num=num)
+             num=num, inst_node_ptr=pb.get("inst_node_ptr"))
     has_loads = "load" in pb and len(pb["load"]) > 0
     m.set_loads(eload=pb.get("eload"), eloadp=pb.get("eloadp"), nload=pb.get("nload"),
                 f=pb.get("f"), load=pb["load"] if has_loads else None,

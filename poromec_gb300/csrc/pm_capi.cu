@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 
 #include "pm_internal.h"
 
@@ -556,7 +557,7 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   if (const char* env = std::getenv("PM_SPMV_SHAPE")) {
     const int u = std::atoi(env);
     for (int c : pm::kCfShapes)
-      if (u == c && !(c == pm::kCaShape && h->P.ca_warps == 0)) {
+      if (u == c && !(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0))) {
         h->shape = u;
         return PM_OK;
       }
@@ -566,7 +567,9 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   float best = 0.f;
   int best_c = 1;
   for (int c : pm::kCfShapes) {
-    if (c == pm::kCaShape && h->P.ca_warps == 0) continue;  // records do not fit in smem
+    // the record kernel: only where two records per warp fit in shared
+    // memory, and not for batches (it does not skip converged instances)
+    if (c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) continue;
     const pm::CompVals C = h->P.comp(c);
     PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
     PM_CUDA(cudaEventRecord(h->ev[0], s));
@@ -594,13 +597,13 @@ int ensure_comp(Handle* h, cudaStream_t s) {
   if (!h->P.valh) {
     PM_CUDA(cudaMalloc(&h->P.valh, sizeof(float) * (size_t)h->P.nnz));
     PM_CUDA(cudaMalloc(&h->P.vall, sizeof(int8_t) * (size_t)h->P.nnz));
-    PM_TRY(pm::build_rec_layout(h));
+    if (h->ninst == 0) PM_TRY(pm::build_rec_layout(h));  // batches do not use records
   }
   if (h->shape != pm::kCaShape) {
     h->launches += 1;
     PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
   }
-  if (h->shape == 0 || h->shape == pm::kCaShape) {
+  if (h->P.rec && (h->shape == 0 || h->shape == pm::kCaShape)) {
     h->launches += 1;
     PM_CUDA(pm::split_records(h->P.view(), h->P.val, h->P.comp(h->shape), s));
   }
@@ -624,6 +627,199 @@ int spmv_op(Handle* h, const double* d_x, double* d_y, cudaStream_t s) {
   return PM_OK;
 }
 
+// ---- batches of independent meshes -------------------------------------------
+// Device tables of the segmented layout (BatchView) from the equation
+// ranges of the instances; equations are numbered in node order, so each
+// instance's equations are one contiguous range.
+int batch_setup(Handle* h) {
+  const int ni = h->ninst;
+  std::vector<int32_t> lo(ni, 0x7fffffff), hi(ni, -1);
+  for (int i = 0; i < ni; ++i)
+    for (int n = h->h_inst_node[i]; n < h->h_inst_node[i + 1]; ++n)
+      for (int j = 0; j < 4; ++j) {
+        const int e = h->h_eq[(size_t)4 * n + j];
+        if (e > 0) {
+          lo[i] = std::min(lo[i], e - 1);
+          hi[i] = std::max(hi[i], e);
+        }
+      }
+  h->h_inst_eq.assign(ni + 1, 0);
+  for (int i = 0; i < ni; ++i) {
+    if (hi[i] < 0) {  // no free equation
+      lo[i] = h->h_inst_eq[i];
+      hi[i] = h->h_inst_eq[i];
+    }
+    if (lo[i] != h->h_inst_eq[i]) {
+      h->err = "batch: the equations of an instance are not one contiguous range";
+      return PM_E_ARG;
+    }
+    h->h_inst_eq[i + 1] = hi[i];
+  }
+  if (h->h_inst_eq[ni] != h->neq) {
+    h->err = "batch: equation ranges do not cover the system";
+    return PM_E_ARG;
+  }
+  pm::BatchView& B = h->B;
+  B.ninst = ni;
+  B.chunk = 2048;
+  std::vector<int32_t> bptr(ni + 1, 0), binst;
+  for (int i = 0; i < ni; ++i) {
+    const int cnt = h->h_inst_eq[i + 1] - h->h_inst_eq[i];
+    const int nb = std::max(1, (cnt + B.chunk - 1) / B.chunk);
+    bptr[i + 1] = bptr[i] + nb;
+    for (int k = 0; k < nb; ++k) binst.push_back(i);
+  }
+  B.nblk = bptr[ni];
+  auto up = [&](auto** dst, const auto* src, size_t n) -> int {
+    using T = std::remove_pointer_t<std::remove_reference_t<decltype(*dst)>>;
+    if (cudaMalloc((void**)dst, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
+      h->err = "cudaMalloc failed";
+      return PM_E_NOMEM;
+    }
+    if (src) {
+      if (cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+        h->err = "cudaMemcpy failed";
+        return PM_E_CUDA;
+      }
+    } else {
+      cudaMemset(*dst, 0, sizeof(T) * std::max<size_t>(n, 1));
+    }
+    return PM_OK;
+  };
+  int32_t *eq_ptr, *blk_ptr, *blk_inst;
+  PM_TRY(up(&eq_ptr, h->h_inst_eq.data(), (size_t)ni + 1));
+  PM_TRY(up(&blk_ptr, bptr.data(), (size_t)ni + 1));
+  PM_TRY(up(&blk_inst, binst.data(), binst.size()));
+  B.eq_ptr = eq_ptr;
+  B.blk_ptr = blk_ptr;
+  B.blk_inst = blk_inst;
+  PM_TRY(up(&B.bs, (pm::BatchScalars*)nullptr, (size_t)ni));
+  PM_TRY(up(&B.done, (int*)nullptr, (size_t)ni));
+  PM_TRY(up(&B.nactive, (int*)nullptr, 1));
+  PM_TRY(up(&B.partial, (double*)nullptr, (size_t)2 * B.nblk));
+  PM_TRY(up(&B.counter, (unsigned*)nullptr, (size_t)ni));
+  PM_TRY(up(&h->P.node_inst, h->h_inst_act.data(), h->h_inst_act.size()));
+  h->P.inst_done = B.done;
+  PM_TRY(up(&h->d_insweep, (int*)nullptr, (size_t)ni));
+  PM_TRY(up(&h->d_conv0, (double*)nullptr, (size_t)ni));
+  PM_TRY(up(&h->d_bnorms, (double*)nullptr, (size_t)2 * ni));
+  h->b_iters.assign(ni, 0);
+  h->b_nlit.assign(ni, 0);
+  return PM_OK;
+}
+
+// Independent PCG solves of the active instances (active[i] != 0) on the
+// union system; inactive instances get x = 0.  comp: the compensated FP32
+// operator inside the FP64 refinement of krylov(), per instance: after the
+// sweep, r = b - A64 x in FP64, and the instances whose sqrt|(r, m r)| is
+// still above their first sweep's target solve A dx = r to that target.
+int krylov_batch(Handle* h, const double* d_b, double* d_x, double tol, int maxit, bool comp,
+                 const std::vector<int>& active, pm_step_info* info) {
+  const int n = h->neq, ni = h->ninst;
+  pm::KrylovVecs& V = h->D.kv;
+  float2* pair = h->D.kv32.c;
+  const pm::PanelView PB = h->P.bview();
+  const pm::PanelView P = h->P.view();
+  const pm::CompVals C = h->P.comp(h->shape);
+  const pm::BatchView& B = h->B;
+  cudaStream_t s = h->stream;
+  cudaGraphExec_t* g = comp ? &h->bpcgc_graph : &h->bpcg_graph;
+  if (!*g) {
+    PM_TRY(capture(h, g, [&]() {
+      return pm::bpcg_iteration(PB, h->P.val, comp ? &C : nullptr, B, h->D.m, V, pair, s);
+    }));
+  }
+  cudaEvent_t e0 = h->ev[0], e1 = h->ev[1];
+  PM_CUDA(cudaEventRecord(e0, s));
+  PM_CUDA(cudaMemsetAsync(d_x, 0, sizeof(double) * n, s));
+  std::vector<int> insweep(active);
+  std::vector<double> conv0(ni, 0.0), rn2(ni, 0.0);
+  std::vector<pm::BatchScalars> bs(ni);
+  std::vector<int> total(ni, 0);
+  const int kMaxSweeps = 8;
+  int sweeps = 0;
+  for (;;) {
+    PM_CUDA(cudaMemcpyAsync(h->d_insweep, insweep.data(), sizeof(int) * ni,
+                            cudaMemcpyHostToDevice, s));
+    PM_CUDA(cudaMemsetAsync(B.nactive, 0, sizeof(int), s));
+    h->launches += 1;
+    PM_CUDA(pm::bpcg_init(B, sweeps == 0 ? d_b : h->D.rr, h->D.m, V, comp ? pair : nullptr, tol,
+                          sweeps == 0 ? nullptr : h->d_conv0, h->d_insweep, maxit, s));
+    for (int launched = 0;; launched += kGraphIters) {
+      int nact = 0;
+      PM_CUDA(cudaMemcpyAsync(&nact, B.nactive, sizeof(int), cudaMemcpyDeviceToHost, s));
+      PM_CUDA(cudaStreamSynchronize(s));
+      if (nact == 0) break;
+      if (launched > maxit + kGraphIters) {  // every instance stops at maxit
+        h->err = "batch PCG: iteration count past maxit with instances still active";
+        return PM_E_NOCONV;
+      }
+      PM_CUDA(cudaGraphLaunch(*g, s));
+      h->launches += 4 * kGraphIters;
+    }
+    PM_CUDA(cudaMemcpyAsync(bs.data(), B.bs, sizeof(pm::BatchScalars) * ni,
+                            cudaMemcpyDeviceToHost, s));
+    PM_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < ni; ++i) {
+      if (!insweep[i]) continue;
+      total[i] += bs[i].iter;
+      if (bs[i].conv_flag == 3 || bs[i].conv_flag == 2) {
+        h->err = "batch PCG, instance " + std::to_string(i) +
+                 (bs[i].conv_flag == 3 ? ": breakdown (non-finite recurrence)"
+                                       : ": no convergence reached after " +
+                                             std::to_string(total[i]) + " iterations");
+        if (info) info->iters = total[i];
+        return PM_E_NOCONV;
+      }
+      if (sweeps == 0) conv0[i] = bs[i].conv;
+    }
+    h->launches += 1;
+    PM_CUDA(pm::baxpy(B, d_x, V.x, h->d_insweep, s));
+    ++sweeps;
+    if (!comp) break;
+    // FP64 outer residual of every instance in the sweep
+    h->launches += 2;
+    PM_CUDA(pm::spmv(P, h->P.val, d_x, h->D.dx, 0, nullptr, nullptr, nullptr, s));
+    PM_CUDA(pm::btrue_residual(B, d_b, h->D.dx, h->D.m, h->D.rr, h->d_bnorms, s));
+    PM_CUDA(cudaMemcpyAsync(rn2.data(), h->d_bnorms, sizeof(double) * ni,
+                            cudaMemcpyDeviceToHost, s));
+    PM_CUDA(cudaStreamSynchronize(s));
+    int again = 0;
+    for (int i = 0; i < ni; ++i) {
+      insweep[i] = insweep[i] && !(std::sqrt(std::fabs(rn2[i])) < conv0[i]) && conv0[i] > 0.0;
+      again += insweep[i];
+    }
+    if (h->debug)
+      fprintf(stderr, "batch refine sweep %d: %d instances above target\n", sweeps, again);
+    if (again == 0) break;
+    if (sweeps >= kMaxSweeps) {
+      h->err = "batch refinement: FP64 residual above target after " +
+               std::to_string(sweeps) + " sweeps";
+      return PM_E_NOCONV;
+    }
+    PM_CUDA(cudaMemcpyAsync(h->d_conv0, conv0.data(), sizeof(double) * ni,
+                            cudaMemcpyHostToDevice, s));
+  }
+  PM_CUDA(cudaEventRecord(e1, s));
+  PM_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  int mx = 0;
+  for (int i = 0; i < ni; ++i) {
+    h->b_iters[i] = total[i];
+    mx = std::max(mx, total[i]);
+  }
+  h->timers[5] = ms;
+  h->timers[6] = mx;
+  if (info) {
+    info->iters = mx;
+    info->refine = comp ? sweeps : 0;
+    info->conv = 0.0;
+    info->xkx = 0.0;
+  }
+  return PM_OK;
+}
+
 int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x, double tol,
               int maxit, pm_step_info* info) {
   if (!h->assembled) {
@@ -631,6 +827,15 @@ int solve_dev(Handle* h, int solver, int precond, const double* d_b, double* d_x
     return PM_E_STATE;
   }
   PM_TRY(build_precond(h, precond));
+  if (h->ninst > 0) {
+    if (solver != 1 || h->precision == PM_FP32_REFINE) {
+      h->err = "a batch of meshes is solved by PCG (solver 1) in PM_FP64 or PM_FP32C_REFINE";
+      return PM_E_ARG;
+    }
+    const bool comp = h->precision == PM_FP32C_REFINE;
+    if (comp) PM_TRY(ensure_comp(h, h->stream));
+    return krylov_batch(h, d_b, d_x, tol, maxit, comp, std::vector<int>(h->ninst, 1), info);
+  }
   if (h->precision == PM_FP32_REFINE) {
     if (!h->assembled32) {
       if (!h->P.val32) {
@@ -722,6 +927,13 @@ void free_all(Handle* h) {
   if (h->pcgm_graph) cudaGraphExecDestroy(h->pcgm_graph);
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
   if (h->pcgc_graph) cudaGraphExecDestroy(h->pcgc_graph);
+  if (h->bpcg_graph) cudaGraphExecDestroy(h->bpcg_graph);
+  if (h->bpcgc_graph) cudaGraphExecDestroy(h->bpcgc_graph);
+  for (void* p : {(void*)h->B.eq_ptr, (void*)h->B.blk_ptr, (void*)h->B.blk_inst, (void*)h->B.bs,
+                  (void*)h->B.done, (void*)h->B.nactive, (void*)h->B.partial,
+                  (void*)h->B.counter, (void*)h->P.node_inst, (void*)h->d_insweep,
+                  (void*)h->d_conv0, (void*)h->d_bnorms})
+    if (p) cudaFree(p);
   if (h->minresc_graph) cudaGraphExecDestroy(h->minresc_graph);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
@@ -767,6 +979,149 @@ int set_dev_array(Handle* h, T** dst, const T* src, size_t n) {
   return PM_OK;
 }
 
+// One step of every instance of a batch: the 'solv' macro of pm_step with
+// each instance's own nonlinear test (cal_residuo_pm per instance: its own
+// reference norms, its own decision); instances that have met their test
+// take no further solve (their correction is zero), the others solve
+// together in one batched PCG.
+int step_batch(Handle* h, int maxnlit, double tol, int stop_crit, int solver, int precond,
+               double solvtol, int maxit, int reassemble, pm_step_info* info) {
+  if (solver != 1 || h->precision == PM_FP32_REFINE) {
+    h->err = "a batch of meshes is solved by PCG (solver 1) in PM_FP64 or PM_FP32C_REFINE";
+    return PM_E_ARG;
+  }
+  cudaStream_t s = h->stream;
+  pm::Dev& D = h->D;
+  const int ni = h->ninst;
+  const int64_t launches0 = h->launches;
+  cudaEvent_t ev[4];
+  for (auto& e : ev) PM_CUDA(cudaEventCreate(&e));
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
+    }
+  } guard{ev};
+  h->istep += 1;
+  h->t = h->t + h->dt;
+  PM_CUDA(cudaEventRecord(ev[0], s));
+  h->launches += 2 + (h->fstress0 ? 1 : 0);
+  k_pload<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.nload, D.f, D.u, D.b0,
+                                              D.load, D.fload, h->maxt, D.x, h->t, h->dt,
+                                              h->gravity_mod);
+  PM_CUDA(cudaGetLastError());
+  PM_TRY(rhs4(h, D.u, D.b0));
+  if (h->fstress0) PM_CUDA(pm::axpy_into(h->neq, D.b0, D.bst0, 1.0, s));
+  k_predict<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0);
+  PM_CUDA(cudaGetLastError());
+  PM_CUDA(cudaEventRecord(ev[1], s));
+  std::vector<int> active(ni, 1);
+  std::vector<double> nr(2 * (size_t)ni);
+  h->b_res0.resize(ni);
+  h->b_resu0.resize(ni);
+  h->b_resp0.resize(ni);
+  h->b_nlit.assign(ni, 0);
+  std::fill(h->b_iters.begin(), h->b_iters.end(), 0);
+  std::vector<int> iters(ni, 0);
+  bool lhs = true;
+  int it = 1;
+  pm_step_info loc{};
+  double t_asm = 0, t_res = 0, t_sol = 0;
+  for (;;) {
+    PM_CUDA(cudaMemcpyAsync(D.b, D.b0, sizeof(double) * h->neq, cudaMemcpyDeviceToDevice, s));
+    PM_CUDA(cudaEventRecord(ev[2], s));
+    const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
+    if (need_K) {
+      PM_TRY(assemble_K(h, false));
+      h->assembled32 = h->assembledC = false;
+    }
+    PM_TRY(residual(h, D.u, D.b));
+    PM_CUDA(cudaEventRecord(ev[3], s));
+    PM_TRY(check_elem_err(h));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[2], ev[3]);
+    t_asm += ms;
+    if (stop_crit == 1 || stop_crit == 2) {
+      h->launches += 1;
+      PM_CUDA(pm::bresnorms(h->B, D.b, D.dofkind, h->d_bnorms, s));
+      PM_CUDA(cudaMemcpyAsync(nr.data(), h->d_bnorms, sizeof(double) * 2 * ni,
+                              cudaMemcpyDeviceToHost, s));
+      PM_CUDA(cudaStreamSynchronize(s));
+      int left = 0;
+      for (int i = 0; i < ni; ++i) {
+        if (!active[i]) continue;
+        bool done = false;
+        if (stop_crit == 1) {  // cal_residuo_pm (Residuo.f:39-276), per instance
+          const double res = std::sqrt(nr[2 * i] + nr[2 * i + 1]);
+          if (it == 1) h->b_res0[i] = res;
+          else if (it == 2) h->b_res0[i] = std::max(h->b_res0[i], res);
+          loc.res_u = std::max(loc.res_u, res);
+          done = h->b_res0[i] > 0.0 ? res / h->b_res0[i] < tol : true;
+        } else {
+          const double gresu = std::sqrt(nr[2 * i]), gresp = std::sqrt(nr[2 * i + 1]);
+          if (it == 1) {
+            h->b_resu0[i] = gresu;
+            h->b_resp0[i] = gresp;
+          } else if (it == 2) {
+            h->b_resu0[i] = std::max(h->b_resu0[i], gresu);
+            h->b_resp0[i] = std::max(h->b_resp0[i], gresu);  // as the reference
+          }
+          int istop = 0;
+          if (gresu / h->b_resu0[i] < tol) istop += 1;
+          if (gresp / h->b_resp0[i] < tol) istop += 1;
+          done = istop == 2;
+        }
+        if (done) {
+          active[i] = 0;
+          h->b_nlit[i] = it;
+        } else {
+          ++left;
+        }
+      }
+      if (left == 0) break;
+    }
+    PM_CUDA(cudaEventRecord(ev[2], s));
+    PM_TRY(build_precond(h, precond));
+    const bool comp = h->precision == PM_FP32C_REFINE;
+    if (comp) PM_TRY(ensure_comp(h, s));
+    pm_step_info si{};
+    PM_TRY(krylov_batch(h, D.b, D.xs, solvtol, maxit, comp, active, &si));
+    for (int i = 0; i < ni; ++i)
+      if (active[i]) iters[i] += h->b_iters[i];
+    loc.iters = std::max(loc.iters, si.iters);
+    loc.refine = si.refine;
+    h->launches += 1;
+    k_delta_update<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.u, D.xs);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(cudaEventRecord(ev[3], s));
+    PM_CUDA(cudaEventSynchronize(ev[3]));
+    cudaEventElapsedTime(&ms, ev[2], ev[3]);
+    t_sol += ms;
+    if (it >= maxnlit) {
+      h->err = "nonlinear iteration: no convergence after " + std::to_string(it) +
+               " iterations (batch)";
+      return PM_E_NLNOCONV;
+    }
+    ++it;
+    lhs = false;
+  }
+  h->b_iters = iters;
+  loc.nlit = it;
+  h->launches += 1;
+  k_update_res<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0, D.dp);
+  PM_CUDA(cudaGetLastError());
+  PM_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev[0], ev[1]);
+  h->timers[0] = ms;
+  h->timers[1] = t_asm;
+  h->timers[2] = 0.0;
+  h->timers[3] = t_sol;
+  h->timers[7] = (double)(h->launches - launches0);
+  if (info) *info = loc;
+  return PM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -793,10 +1148,11 @@ const char* pm_last_error(pm_handle hh) {
   return h ? h->err.c_str() : "null handle";
 }
 
-int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
-                   const int32_t* ix, const int32_t* id, const int32_t* fnno, const double* x,
-                   int numat, const int32_t* ie, const double* e, const int32_t* num,
-                   pm_handle* out) {
+static int mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
+                       const int32_t* ix, const int32_t* id, const int32_t* fnno,
+                       const double* x, int numat, const int32_t* ie, const double* e,
+                       const int32_t* num, int ninst, const int32_t* inst_node_ptr,
+                       pm_handle* out) {
   if (!out || !ix || !id || !fnno || !x || !ie || !e || nnode <= 0 || numel <= 0 ||
       numat <= 0 || ndm != 3 || ndf != 4 ||
       !((nen == 20 && nenv == 8) || (nen == 10 && nenv == 4)))
@@ -807,6 +1163,20 @@ int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
   for (int el = 0; el < numel; ++el) {
     const int ma = ix[(size_t)(nen + 1) * el + nen];
     if (ma < 1 || ma > numat) return PM_E_ARG;
+  }
+  if (ninst > 0) {
+    // node ranges 0 = p[0] <= ... <= p[ninst] = nnode; every element inside one range
+    if (!inst_node_ptr || num || inst_node_ptr[0] != 0 || inst_node_ptr[ninst] != nnode)
+      return PM_E_ARG;
+    for (int i = 0; i < ninst; ++i)
+      if (inst_node_ptr[i + 1] < inst_node_ptr[i]) return PM_E_ARG;
+    const int32_t* pe = inst_node_ptr + ninst + 1;
+    for (int el = 0; el < numel; ++el) {
+      const int32_t* nd = ix + (size_t)(nen + 1) * el;
+      const int i0 = (int)(std::upper_bound(inst_node_ptr, pe, nd[0] - 1) - inst_node_ptr) - 1;
+      for (int a = 0; a < nen; ++a)
+        if (nd[a] - 1 < inst_node_ptr[i0] || nd[a] - 1 >= inst_node_ptr[i0 + 1]) return PM_E_ARG;
+    }
   }
   Handle* h = new (std::nothrow) Handle();
   if (!h) return PM_E_NOMEM;
@@ -819,6 +1189,10 @@ int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
   h->hexa = (nen == 20);
   h->h_e.assign(e, e + (size_t)PM_PROP * numat);
   h->h_ie.assign(ie, ie + numat);
+  if (ninst > 0) {
+    h->ninst = ninst;
+    h->h_inst_node.assign(inst_node_ptr, inst_node_ptr + ninst + 1);
+  }
   int st = PM_OK;
   auto fail = [&](int s) {
     free_all(h);
@@ -832,8 +1206,36 @@ int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
   if ((st = pm::build_structure(h, ix, id, fnno, x, num)) != PM_OK) return fail(st);
   if ((st = alloc_state(h)) != PM_OK) return fail(st);
   if ((st = upload_materials(h)) != PM_OK) return fail(st);
+  if (ninst > 0 && (st = batch_setup(h)) != PM_OK) return fail(st);
   h->debug = getenv("PM_DEBUG") != nullptr;
   *out = reinterpret_cast<pm_handle>(h);
+  return PM_OK;
+}
+
+int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
+                   const int32_t* ix, const int32_t* id, const int32_t* fnno, const double* x,
+                   int numat, const int32_t* ie, const double* e, const int32_t* num,
+                   pm_handle* out) {
+  return mesh_create(nnode, nnodev, numel, nen, nenv, ndm, ndf, ix, id, fnno, x, numat, ie, e,
+                     num, 0, nullptr, out);
+}
+
+int pm_batch_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
+                    const int32_t* ix, const int32_t* id, const int32_t* fnno, const double* x,
+                    int numat, const int32_t* ie, const double* e, int ninst,
+                    const int32_t* inst_node_ptr, pm_handle* out) {
+  if (ninst < 1) return PM_E_ARG;
+  return mesh_create(nnode, nnodev, numel, nen, nenv, ndm, ndf, ix, id, fnno, x, numat, ie, e,
+                     nullptr, ninst, inst_node_ptr, out);
+}
+
+int pm_get_batch_iters(pm_handle hh, int* iters, int* nlit, int n) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || h->ninst == 0 || n < h->ninst) return PM_E_ARG;
+  for (int i = 0; i < h->ninst; ++i) {
+    if (iters) iters[i] = h->b_iters[i];
+    if (nlit) nlit[i] = h->b_nlit[i];
+  }
   return PM_OK;
 }
 
@@ -1085,6 +1487,9 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
             double solvtol, int maxit, int reassemble, pm_step_info* info) {
   Handle* h = reinterpret_cast<Handle*>(hh);
   if (!h || maxnlit < 1 || maxit < 1) return PM_E_ARG;
+  if (h->ninst > 0)
+    return step_batch(h, maxnlit, tol, stop_crit, solver, precond, solvtol, maxit, reassemble,
+                      info);
   cudaStream_t s = h->stream;
   pm::Dev& D = h->D;
   cudaEvent_t ev[6];

@@ -52,11 +52,18 @@ struct Panels {
   uint8_t* rec = nullptr;
   int64_t* rec_off = nullptr;
   int rec_max = 0, ca_warps = 0, ca_grid = 0;
+  // batches: instance of each active node, done flag of each instance
+  int32_t* node_inst = nullptr;
+  int* inst_done = nullptr;
   // indexed by node id - 1
   int64_t* node_val_off = nullptr;
   int32_t* node_W = nullptr;
   PanelView view() const {
-    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols};
+    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols, nullptr, nullptr};
+  }
+  // the view of the batched iteration: rows of converged instances skipped
+  PanelView bview() const {
+    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols, node_inst, inst_done};
   }
   CompVals comp(int shape) const {
     return CompVals{valh, vall, rec, rec_off, rec_max, ca_warps, ca_grid, shape};
@@ -140,6 +147,18 @@ struct Handle {
   // host copies of the panel structure (pm_get_csrd)
   std::vector<int32_t> h_eq0, h_d, h_W, h_low, h_cols;
   std::vector<int32_t> h_order;    // SpMV visiting order of the active nodes
+  // batch of independent meshes (pm_batch_create); ninst = 0 for one mesh
+  int ninst = 0;
+  std::vector<int32_t> h_inst_node;  // ninst + 1 node ranges (0-based)
+  std::vector<int32_t> h_inst_act;   // instance of each active node
+  std::vector<int32_t> h_inst_eq;    // ninst + 1 equation ranges (0-based)
+  BatchView B{};
+  int* d_insweep = nullptr;
+  double* d_conv0 = nullptr;
+  double* d_bnorms = nullptr;
+  std::vector<double> b_res0, b_resu0, b_resp0;
+  std::vector<int> b_iters;          // Krylov iterations of the last solve, per instance
+  std::vector<int> b_nlit;           // nonlinear iterations of the last step, per instance
   std::vector<int64_t> h_val_off, h_col_off;
   int nloads = 0, maxt = 1;
   double gravity[3] = {0.0, 0.0, -9.81};
@@ -161,6 +180,7 @@ struct Handle {
   // handle's lifetime)
   cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr, pcgm_graph = nullptr;
   cudaGraphExec_t pcgc_graph = nullptr, minresc_graph = nullptr;
+  cudaGraphExec_t bpcg_graph = nullptr, bpcgc_graph = nullptr;
   double timers[8] = {0};
   int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;

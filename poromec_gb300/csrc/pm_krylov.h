@@ -21,6 +21,11 @@ struct PanelView {
   const int64_t* val_off;  // value offset
   const int64_t* col_off;  // column list offset
   const int32_t* cols;     // 0-based column equations
+  // batches of independent meshes: the instance of each active node, and the
+  // instances whose solve has converged (their rows are skipped); both null
+  // for a single mesh
+  const int32_t* node_inst;
+  const int* inst_done;
 };
 
 // Scalars of one Krylov solve, kept in device memory so that a captured
@@ -131,5 +136,44 @@ cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const doubl
 cudaError_t true_residual(int n, const double* b, const double* q, const double* m, int absval,
                           double* r, double* out, double* partial, unsigned* counter,
                           cudaStream_t s);
+
+// ---- batches of independent meshes (pm_batch.cu) ------------------------------
+// The instances are held as one union mesh; their equations are contiguous
+// ranges.  Per-instance dot products are segmented reductions: each block
+// takes a chunk of one instance's range, and the last block of an instance
+// sums the instance's block partials in block order (deterministic).
+struct BatchScalars {
+  double d, bmb, conv, alpha, beta, pq;
+  int iter, conv_flag, maxit, pad;
+};
+
+struct BatchView {
+  int ninst;
+  int nblk;                 // blocks of the segmented layout
+  int chunk;                // equations per block
+  const int32_t* eq_ptr;    // ninst + 1 equation ranges
+  const int32_t* blk_ptr;   // ninst + 1 block ranges
+  const int32_t* blk_inst;  // instance of each block
+  BatchScalars* bs;         // per instance
+  int* done;                // per instance: solve finished (or not in this sweep)
+  int* nactive;             // instances still iterating
+  double* partial;          // 2 * nblk
+  unsigned* counter;        // per instance
+};
+
+cudaError_t bpcg_init(const BatchView& B, const double* b, const double* m, KrylovVecs& V,
+                      float2* pair, double tol, const double* conv_abs, const int* insweep,
+                      int maxit, cudaStream_t s);
+// one iteration: q = A p (FP64 panels, or the compensated operator when
+// C != nullptr), then the per-instance alpha, update and direction
+cudaError_t bpcg_iteration(const PanelView& P, const double* val64, const CompVals* C,
+                           const BatchView& B, const double* m, KrylovVecs& V, float2* pair,
+                           cudaStream_t s);
+cudaError_t bresnorms(const BatchView& B, const double* b, const int32_t* kind, double* out,
+                      cudaStream_t s);
+cudaError_t btrue_residual(const BatchView& B, const double* b, const double* q,
+                           const double* m, double* r, double* out, cudaStream_t s);
+cudaError_t baxpy(const BatchView& B, double* y, const double* x, const int* mask,
+                  cudaStream_t s);
 
 }  // namespace pm

@@ -166,12 +166,22 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
   // panels and their column lists are stored in this order, so the SpMV
   // streams them sequentially (a scattered visit over GBs of panels costs
   // DRAM pages and TLB reach).
-  std::vector<int32_t> order(nact);
+  // For a batch of meshes the instance comes first, so that an instance's
+  // nodes are contiguous in the order and a converged instance's panels are
+  // skipped as one stretch.
+  std::vector<int32_t> order(nact), inst_act(nact, 0);
+  if (h->ninst > 0)
+    for (int k = 0; k < nact; ++k)
+      inst_act[k] = (int32_t)(std::upper_bound(h->h_inst_node.begin(), h->h_inst_node.end(),
+                                               act[k]) -
+                              h->h_inst_node.begin()) - 1;
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (inst_act[a] != inst_act[b]) return inst_act[a] < inst_act[b];
     if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
     return h->h_W[a] > h->h_W[b];
   });
+  h->h_inst_act = inst_act;
   for (int i = 0; i < nact; ++i) {
     const int k = order[i];
     const int n = act[k];

@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256)
     const int node = slot < P.nact ? P.order[slot] : 0;
     int e0 = 0, d = 0, W = 0;
     T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-    if (slot < P.nact) {
+    if (slot < P.nact && !(P.inst_done && P.inst_done[P.node_inst[node]])) {
       e0 = P.eq0[node];
       d = P.d[node];
       W = P.W[node];
@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(256)
     const int node = slot < P.nact ? P.order[slot] : 0;
     int e0 = 0, d = 0, W = 0;
     F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    if (slot < P.nact) {
+    if (slot < P.nact && !(P.inst_done && P.inst_done[P.node_inst[node]])) {
       e0 = P.eq0[node];
       d = P.d[node];
       W = P.W[node];

@@ -291,3 +291,75 @@ def tetra_problem(n=48, seed=7, steps=30):
     return _finish(m, idf, e, np.zeros((m["numel"], 7), np.int32), load, fload, u0,
                    [0.0, 0.0, -g], 60.0, nload=nload, nsteps=steps, solver=7, precond=2,
                    solvtol=1e-8, maxit=100000, maxnlit=2, name="tetra10 Kuhn %d^3" % n)
+
+
+def batch_instances(ninst=96, nmin=8, nmax=32, seed=4242):
+    """Instances of the batched workload: ninst unit cubes, structured
+    hexa20 with an edge count drawn uniformly from nmin..nmax, each with its
+    own E (lognormal, median 1 GPa, sigma_ln 0.3) and log k (normal, mean
+    ln 1e-14 m^2, sigma 1; mu = 1e-3 Pa s), nu = 0.25, alpha = 1,
+    M = 1e4 MPa, and the loading of the consolidation column: lateral
+    rollers, base fixed in z, drained top, 1 MPa top load from t = 0,
+    hydrostatic initial pressure, dt = 10 s."""
+    rng = np.random.default_rng(seed)
+    out = []
+    rho_f, g, mu = 1000.0, 10.0, 1.0e-3
+    for _ in range(ninst):
+        n = int(rng.integers(nmin, nmax + 1))
+        E = 1000.0 * float(np.exp(0.3 * rng.standard_normal()))
+        k = float(np.exp(np.log(1e-14) + rng.standard_normal()))
+        m = hexa20_box(n, n, n, 1.0, 1.0, 1.0)
+        x = m["x"]
+        tol = 1e-9
+        idf = np.zeros((m["nnode"], 4), np.int32)
+        idf[np.abs(x[:, 0]) < tol, 0] = 1
+        idf[np.abs(x[:, 0] - 1.0) < tol, 0] = 1
+        idf[np.abs(x[:, 1]) < tol, 1] = 1
+        idf[np.abs(x[:, 1] - 1.0) < tol, 1] = 1
+        idf[np.abs(x[:, 2]) < tol, 2] = 1
+        top = np.abs(x[:, 2] - 1.0) < tol
+        idf[top & (m["fnno"] == 1), 3] = 1
+        e = material_row(E, 0.25, conductivity(k / mu, rho_f, g), 1.0e4, 1.0, 0.0, rho_f)[None]
+        load, fload = _load_table([0.0], [[0.0, 0.0, -1.0]])
+        u0 = np.zeros((m["nnode"], 4))
+        u0[:, 3] = rho_f * 1e-6 * g * (1.0 - x[:, 2]) * m["fnno"]
+        u0[idf[:, 3] == 1, 3] = 0.0
+        out.append(_finish(m, idf, e, _faces_top_hexa(m), load, fload, u0, [0.0, 0.0, -g],
+                           10.0, nsteps=20, solver=1, precond=2, solvtol=1e-10, maxit=50000,
+                           maxnlit=2, name="batch instance hexa20 %d^3" % n, n=n))
+    return out
+
+
+def union_problem(instances):
+    """One problem holding independent instances side by side (node ids
+    offset, one material per instance, the load table of the first
+    instance, which all instances share) with their node ranges in
+    inst_node_ptr, for a batched handle."""
+    ptr = [0]
+    ix, x, fnno, idf, u0, eload, e = [], [], [], [], [], [], []
+    for k, pb in enumerate(instances):
+        off = ptr[-1]
+        a = pb["ix"].copy()
+        a[:, :pb["nen"]] += off
+        a[:, pb["nen"]] = k + 1
+        ix.append(a)
+        x.append(pb["x"])
+        fnno.append(pb["fnno"])
+        idf.append(pb["id"])
+        u0.append(pb["u0"])
+        eload.append(pb["eload"])
+        e.append(np.asarray(pb["e"]).reshape(-1, PROP)[0])
+        ptr.append(off + int(pb["nnode"]))
+    first = instances[0]
+    pb = dict(nnode=ptr[-1], nnodev=int(sum(int(p["nnodev"]) for p in instances)),
+              numel=int(sum(int(p["numel"]) for p in instances)), nen=first["nen"],
+              nenv=first["nenv"], ix=np.concatenate(ix), x=np.concatenate(x),
+              fnno=np.concatenate(fnno), id=np.concatenate(idf), u0=np.concatenate(u0),
+              eload=np.concatenate(eload), e=np.stack(e),
+              ie=np.full(len(instances), int(first["ie"][0]), np.int32),
+              load=first["load"], fload=first["fload"], gravity=first["gravity"],
+              dt=first["dt"], inst_node_ptr=np.asarray(ptr, np.int32),
+              nsteps=first.get("nsteps"), solver=1, precond=2, solvtol=first.get("solvtol"),
+              maxit=first.get("maxit"), maxnlit=first.get("maxnlit"),
+              name="batch of %d instances" % len(instances))
+    return pb
