@@ -53,6 +53,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one step of the same workload only (for the ncu launch list)")
+    ap.add_argument("--workload", default="cube", choices=["cube", "batched"],
+                    help="batched: only the batch of independent cubes (its own line)")
+    ap.add_argument("--batch-inst", type=int, default=96)
+    ap.add_argument("--batch-steps", type=int, default=2,
+                    help="timed steps of the batch leg in the default run")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--fp32-plain", action="store_true",
                     help="also time the plain FP32-value refinement (PM_FP32_REFINE)")
     ap.add_argument("--spmv-only", action="store_true",
@@ -267,6 +273,57 @@ def run_spmv_only(args):
           flush=True)
 
 
+def batched_leg(args, steps, warmup):
+    """The batched workload: args.batch_inst independent unit cubes, hexa20
+    n^3 with n uniform in 8..32, per-instance lognormal E and k, the loading
+    of the consolidation column, all stepped by one handle (per-instance
+    PCG, shared graph launches) with the compensated FP32 operator in the
+    FP64 refinement; value = instance-steps per second."""
+    import torch
+    import poromec_gb300 as pg
+    from poromec_gb300 import meshgen
+    t0 = time.perf_counter()
+    inst = meshgen.batch_instances(ninst=args.batch_inst, nmin=8, nmax=32, seed=4242)
+    pb = meshgen.union_problem(inst)
+    m = pg.from_problem(pb)
+    m.set_precision(pg.capi.PM_FP32C_REFINE)
+    t_setup = time.perf_counter() - t0
+    kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=1, precond=2,
+              solvtol=float(pb["solvtol"]), maxit=200000, reassemble=True)
+    for _ in range(warmup):
+        m.step(**kw)
+    torch.cuda.synchronize()
+    its = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.step(**kw)
+        its.append(m.batch_iters()[0].copy())
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    it = np.array(its)
+    ns = np.array([p["n"] for p in inst])
+    out = {"value": len(inst) * steps / el, "unit": "instance-steps/s",
+           "ms_per_step": el / steps * 1e3, "instances": len(inst), "steps": steps,
+           "warmup": warmup, "equations": int(m.neq), "nad": int(m.nad),
+           "edge_min": int(ns.min()), "edge_max": int(ns.max()),
+           "pcg_iterations_max": int(it.max()), "pcg_iterations_mean": float(it.mean()),
+           "operator": "compensated FP32 (FP32 + int8 correction) in FP64 refinement",
+           "solvtol": float(pb["solvtol"]), "setup_s": t_setup,
+           "spmv_shape": m.tune_spmv()}
+    m.close()
+    return out
+
+
+def run_batched(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    b = batched_leg(args, args.steps, args.warmup)
+    if rank == 0:
+        print(json.dumps(dict(metric="batched Biot steps", workload="batched cubes", **b)),
+              flush=True)
+
+
 def run_gpu(args):
     import torch
     rank, world, local = dist_env()
@@ -439,6 +496,9 @@ def run_gpu(args):
         out["fp32_refine"] = mixed
     if plain32:
         out["fp32_plain_refine"] = plain32
+    if not args.no_batch:
+        m.close()  # the batch needs the memory more than the finished cube
+        out["batched"] = batched_leg(args, args.batch_steps, 1)
     if not args.no_cpu:
         t_step, parts, sample, threads = cpu_step_estimate(pb, int(np.mean(iters)))
         out["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads,
@@ -453,6 +513,8 @@ def main():
     args = parse()
     if args.spmv_only:
         run_spmv_only(args)
+    elif args.workload == "batched" and args.impl != "reference":
+        run_batched(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
