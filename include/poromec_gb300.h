@@ -199,6 +199,35 @@ int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* d_ja,
  * The first compensated solve or product runs it implicitly. */
 int pm_tune_spmv(pm_handle h, int* shape);
 
+/* Material table (e, PM_PROP per material) replaced, same numat as at
+ * creation; the next step re-assembles.  With one material per element
+ * (numat = numel) this sets per-element parameters. */
+int pm_set_materials(pm_handle h, const double* e, int numat);
+
+/* Adjoint of the time-stepped solve (no counterpart in the reference).  A
+ * step solves K du = F - A s - g0 for the previous state s = (u, dp), with
+ * A s = [Kuu u_u + Kup dp ; Kpp_perm u_p] and g0 = [-body ; G_k] (the
+ * previous-state terms of pform isw 4), then s += (du, du_p).  The reverse
+ * sweep of a misfit J(u_N) is, for n = N..1, with mu = dJ/du and nu = dJ/ddp
+ * in equation space (mu_N from J, nu_N = 0):
+ *   lam_n = K^-1 (mu_n + nu_n)                       (pm_solve_dev: K = K^T)
+ *   mu_{n-1} = mu_n - [Kuu lam_u ; Kpp_perm lam_p],  nu_{n-1} = nu_n - Kpu lam_u
+ *   grad += contractions of lam_n with the parameter derivatives
+ * Device pointers; stream NULL = the handle's stream (a non-NULL stream is
+ * synchronised before return).  The matrix must be assembled for the step's
+ * dt and materials. */
+/* mu -= [Kuu lam_u ; Kpp_perm lam_p], nu -= Kpu lam_u (lam, mu, nu: neq) */
+int pm_adjoint_apply_dev(pm_handle h, const double* d_lam, double* d_mu, double* d_nu,
+                         void* stream);
+/* grad[3 e + {0, 1, 2}] += d/dlog E, d/dlog k, d/dlog M of the element e
+ * contribution lam^T (F - A s - g0 - K du): -lam_u^T Kuu u_n,
+ * -lam_p^T (Kpp_perm p_n + G_k), lam_p^T Kstor du_p (Kstor = -(1/M) int NN),
+ * with u_n = s + du the step's new state and du its increment, both in the
+ * nodal layout (4 per node); lam: neq; grad: 3 numel (per element when
+ * numat = numel, each element's material parameters). */
+int pm_adjoint_grad_dev(pm_handle h, const double* d_lam, const double* d_un,
+                        const double* d_dun, double* d_grad, void* stream);
+
 /* Timing of the last pm_step phases in milliseconds (CUDA events):
  * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,
  * [3] solve, [4] unused (0), [5] device time of the last Krylov solve,

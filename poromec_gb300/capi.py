@@ -85,6 +85,9 @@ def load(path=None):
     lib.pm_solve_dev.argtypes = [c_p, c_i, c_i, c_p, c_p, c_d, c_i, c_p, c_p]
     lib.pm_matvec_csrd_dev.argtypes = [c_i, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
     lib.pm_get_timers.argtypes = [c_p, c_p, c_i]
+    lib.pm_set_materials.argtypes = [c_p, c_p, c_i]
+    lib.pm_adjoint_apply_dev.argtypes = [c_p] * 5
+    lib.pm_adjoint_grad_dev.argtypes = [c_p] * 6
     _lib = lib
     return lib
 
@@ -193,6 +196,33 @@ class Mesh:
 
     def set_refine(self, inner_tol=1e-5):
         self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
+
+    def set_materials(self, e):
+        """Replace the material table (numat rows of PM_PROP values)."""
+        ea = _f64(e)
+        if ea.ndim == 1:
+            ea = ea.reshape(1, -1)
+        if ea.shape[1] < PM_PROP:
+            ea = np.pad(ea, ((0, 0), (0, PM_PROP - ea.shape[1])))
+        ea = np.ascontiguousarray(ea)
+        self._check(self.lib.pm_set_materials(self.h, _p(ea), ea.shape[0]), "pm_set_materials")
+
+    def adjoint_apply_dev(self, lam_ptr, mu_ptr, nu_ptr, stream=None):
+        """mu -= [Kuu lam_u ; Kpp_perm lam_p], nu -= Kpu lam_u (device pointers)."""
+        self._check(self.lib.pm_adjoint_apply_dev(self.h, ctypes.c_void_p(lam_ptr),
+                                                  ctypes.c_void_p(mu_ptr),
+                                                  ctypes.c_void_p(nu_ptr),
+                                                  ctypes.c_void_p(stream) if stream else None),
+                    "pm_adjoint_apply_dev")
+
+    def adjoint_grad_dev(self, lam_ptr, un_ptr, dun_ptr, grad_ptr, stream=None):
+        """grad += per-element log-parameter contractions (device pointers)."""
+        self._check(self.lib.pm_adjoint_grad_dev(self.h, ctypes.c_void_p(lam_ptr),
+                                                 ctypes.c_void_p(un_ptr),
+                                                 ctypes.c_void_p(dun_ptr),
+                                                 ctypes.c_void_p(grad_ptr),
+                                                 ctypes.c_void_p(stream) if stream else None),
+                    "pm_adjoint_grad_dev")
 
     def batch_iters(self):
         """Per instance of a batch: Krylov iterations of the last solve or

@@ -121,6 +121,16 @@ __global__ void k_delta_update(int nnode, const int32_t* __restrict__ eq,
   }
 }
 
+// equation-space vector -> nodal layout (4 per node), zero on restrained dofs
+__global__ void k_eq_to_nodal(int nnode, const int32_t* __restrict__ eq,
+                              const double* __restrict__ v, double* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * nnode;
+       i += gridDim.x * blockDim.x) {
+    const int k = eq[i];
+    out[i] = k > 0 ? v[k - 1] : 0.0;
+  }
+}
+
 // update_res_v2 (Pload.f:483-540): u = u0 + du, u0 = u, dp += du_p
 __global__ void k_update_res(int nnode, const int32_t* __restrict__ fnno, double* __restrict__ u,
                              double* __restrict__ u0, double* __restrict__ dp) {
@@ -1601,6 +1611,45 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   h->timers[7] = (double)(h->launches - launches0);
   if (info) *info = loc;
   return PM_OK;
+}
+
+int pm_set_materials(pm_handle hh, const double* e, int numat) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !e || numat != h->numat) return PM_E_ARG;
+  h->h_e.assign(e, e + (size_t)PM_PROP * numat);
+  return upload_materials(h);
+}
+
+static int adjoint_launch(Handle* h, int mode, const double* d_lam, const double* d_un,
+                          const double* d_dun, double* d_mu, double* d_nu, double* d_grad,
+                          void* stream) {
+  if (!h->assembled) {
+    h->err = "adjoint before assembly (the element passes use the step's dt)";
+    return PM_E_STATE;
+  }
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  h->launches += 1 + h->numcolors;
+  k_eq_to_nodal<<<grid_for(4 * h->nnode), 256, 0, s>>>(h->nnode, h->D.eq, d_lam, h->D.bx);
+  PM_CUDA(cudaGetLastError());
+  for (int c = 0; c < h->numcolors; ++c)
+    PM_CUDA(pm::launch_adjoint(elem_launch(h, c), h->hexa, mode, h->D.bx, d_un, d_dun, d_mu,
+                               d_nu, d_grad, s));
+  if (stream) PM_CUDA(cudaStreamSynchronize(s));
+  return check_elem_err(h);
+}
+
+int pm_adjoint_apply_dev(pm_handle hh, const double* d_lam, double* d_mu, double* d_nu,
+                         void* stream) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !d_lam || !d_mu || !d_nu) return PM_E_ARG;
+  return adjoint_launch(h, 0, d_lam, nullptr, nullptr, d_mu, d_nu, nullptr, stream);
+}
+
+int pm_adjoint_grad_dev(pm_handle hh, const double* d_lam, const double* d_un,
+                        const double* d_dun, double* d_grad, void* stream) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !d_lam || !d_un || !d_dun || !d_grad) return PM_E_ARG;
+  return adjoint_launch(h, 1, d_lam, d_un, d_dun, nullptr, nullptr, d_grad, stream);
 }
 
 int pm_get_timers(pm_handle hh, double* t, int n) {

@@ -854,6 +854,179 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the time-stepped solve.  Each step solves K du = F - A s - g0
+// with s = (u, dp) the previous state, where (from k_rhs4 and k_residual)
+//   A s = [Kuu u_u + Kup dp ; Kpp_perm u_p],   g0 = [-body ; G_k],
+//   Kpp_perm = -dt perm int(grad N grad N),  G_k = dt perm rho_f int(grad N . g),
+// and then s += (du, du_p).  Every block is linear in one element parameter:
+// Kuu in E, Kpp_perm and G_k in the permeability k, the storage block
+// -(1/M) int(N N) of Kpp in 1/M.
+//
+// MODE 0 (apply), for the adjoint state: mu -= [Kuu lam_u ; Kpp_perm lam_p],
+//   nu -= Kpu lam_u (p rows), element by element (one colour per launch, so
+//   no two elements of a launch share an equation).
+// MODE 1 (grad): per element the contractions of d(F - A s - g0 - K du)
+//   with lam for the log parameters:
+//   d/dlog E:  -lam_u^T Kuu u_n          (u_n = s + du, the step's new state)
+//   d/dlog k:  -lam_p^T (Kpp_perm p_n + G_k)
+//   d/dlog M:   lam_p^T Kstor du_p,  Kstor = -(1/M) int(N N)
+//   accumulated into grad[3 (el - 1) + {0, 1, 2}].
+// ---------------------------------------------------------------------------
+template <bool HEXA>
+struct SmA {
+  Geo<HEXA, double> G;
+  double ll[3 * ET<HEXA>::NEN + ET<HEXA>::NV];  // lam on the element dofs
+  double ul[3 * ET<HEXA>::NEN + ET<HEXA>::NV];  // u_n (MODE 1)
+  double dl[ET<HEXA>::NV];                      // du_p (MODE 1)
+  double S6[ET<HEXA>::NGP][6];
+  double Q4[ET<HEXA>::NGP][4];
+  double gsum[3][ET<HEXA>::NT / 32];
+  ElemCtx E;
+  int sFail;
+};
+
+template <bool HEXA, int MODE>
+__global__ void __launch_bounds__(ET<HEXA>::NT)
+    k_adjoint(ElemLaunch L, const double* __restrict__ lam, const double* __restrict__ un,
+              const double* __restrict__ dun, double* __restrict__ mu, double* __restrict__ nu,
+              double* __restrict__ grad) {
+  constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV, NGP = ET<HEXA>::NGP,
+                NT = ET<HEXA>::NT, NST = 3 * NEN + NV;
+  extern __shared__ __align__(16) unsigned char smem[];
+  SmA<HEXA>& S = *reinterpret_cast<SmA<HEXA>*>(smem);
+  Geo<HEXA, double>& G = S.G;
+  ElemCtx& E = S.E;
+  const int el = L.elems[blockIdx.x];
+  if (threadIdx.x == 0) S.sFail = 0;
+  load_element<HEXA, double>(L, el, E, G);
+  for (int k = threadIdx.x; k < NST; k += NT) {
+    const int n = k < 3 * NEN ? E.nodes[k / 3] : E.nodes[k - 3 * NEN];
+    const int q = k < 3 * NEN ? k % 3 : 3;
+    S.ll[k] = lam[(size_t)kNdf * (n - 1) + q];
+    if (MODE == 1) S.ul[k] = un[(size_t)kNdf * (n - 1) + q];
+  }
+  if (MODE == 1)
+    for (int k = threadIdx.x; k < NV; k += NT) S.dl[k] = dun[(size_t)kNdf * (E.nodes[k] - 1) + 3];
+  __syncthreads();
+  const MatConst mc = L.mat[E.mat - 1];
+  double gE = 0.0, gK = 0.0, gM = 0.0;
+  for (int gq = threadIdx.x; gq < NGP; gq += NT) {
+    if (!point_geometry<HEXA, double>(G, gq, nullptr)) {
+      S.sFail = 1;
+      continue;
+    }
+    // strains, pressure value and gradient of lam (and of u_n)
+    double le[6], ue[6];
+    {
+      double ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
+      double Ux = 0, Uy = 0, Uz = 0, Vx = 0, Vy = 0, Vz = 0, Wx = 0, Wy = 0, Wz = 0;
+#pragma unroll
+      for (int i = 0; i < NEN; ++i) {
+        const double gx = G.g[gq][i][0], gy = G.g[gq][i][1], gz = G.g[gq][i][2];
+        const double a0 = S.ll[3 * i], a1 = S.ll[3 * i + 1], a2 = S.ll[3 * i + 2];
+        ux += gx * a0; uy += gy * a0; uz += gz * a0;
+        vx += gx * a1; vy += gy * a1; vz += gz * a1;
+        wx += gx * a2; wy += gy * a2; wz += gz * a2;
+        if (MODE == 1) {
+          const double b0 = S.ul[3 * i], b1 = S.ul[3 * i + 1], b2 = S.ul[3 * i + 2];
+          Ux += gx * b0; Uy += gy * b0; Uz += gz * b0;
+          Vx += gx * b1; Vy += gy * b1; Vz += gz * b1;
+          Wx += gx * b2; Wy += gy * b2; Wz += gz * b2;
+        }
+      }
+      le[0] = ux; le[1] = vy; le[2] = wz; le[3] = uy + vx; le[4] = vz + wy; le[5] = uz + wx;
+      ue[0] = Ux; ue[1] = Vy; ue[2] = Wz; ue[3] = Uy + Vx; ue[4] = Vz + Wy; ue[5] = Uz + Wx;
+    }
+    double lp = 0, lpx = 0, lpy = 0, lpz = 0, upx = 0, upy = 0, upz = 0, dpv = 0;
+#pragma unroll
+    for (int l = 0; l < NV; ++l) {
+      const double pl = S.ll[3 * NEN + l];
+      lp += G.hp[gq][l] * pl;
+      lpx += G.gp[gq][l][0] * pl; lpy += G.gp[gq][l][1] * pl; lpz += G.gp[gq][l][2] * pl;
+      if (MODE == 1) {
+        const double ql = S.ul[3 * NEN + l];
+        upx += G.gp[gq][l][0] * ql; upy += G.gp[gq][l][1] * ql; upz += G.gp[gq][l][2] * ql;
+        dpv += G.hp[gq][l] * S.dl[l];
+      }
+    }
+    const double w = G.w[gq];
+    const double A = mc.a, B = mc.b, C = mc.c;
+    const double wdp = w * mc.perm * L.dt;
+    if (MODE == 0) {
+      // w D eps(lam) (no coupling term), w dt perm grad lam_p, w alpha div lam_u
+      S.S6[gq][0] = w * (le[0] + B * le[1] + B * le[2]) * A;
+      S.S6[gq][1] = w * (B * le[0] + le[1] + B * le[2]) * A;
+      S.S6[gq][2] = w * (B * le[0] + B * le[1] + le[2]) * A;
+      S.S6[gq][3] = w * le[3] * C * A;
+      S.S6[gq][4] = w * le[4] * C * A;
+      S.S6[gq][5] = w * le[5] * C * A;
+      S.Q4[gq][0] = w * mc.coef_biot * (le[0] + le[1] + le[2]);
+      S.Q4[gq][1] = wdp * lpx; S.Q4[gq][2] = wdp * lpy; S.Q4[gq][3] = wdp * lpz;
+    } else {
+      const double s0 = (ue[0] + B * ue[1] + B * ue[2]) * A;
+      const double s1 = (B * ue[0] + ue[1] + B * ue[2]) * A;
+      const double s2 = (B * ue[0] + B * ue[1] + ue[2]) * A;
+      gE -= w * (le[0] * s0 + le[1] * s1 + le[2] * s2 +
+                 C * A * (le[3] * ue[3] + le[4] * ue[4] + le[5] * ue[5]));
+      gK += wdp * (lpx * (upx - mc.fluid_d * L.g0) + lpy * (upy - mc.fluid_d * L.g1) +
+                   lpz * (upz - mc.fluid_d * L.g2));
+      gM -= w * mc.imod_biot * lp * dpv;
+    }
+  }
+  __syncthreads();
+  if (S.sFail) {
+    if (threadIdx.x == 0) atomicOr(L.err, 1);
+    return;
+  }
+  if (MODE == 1) {
+    double v[3] = {gE, gK, gM};
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double x = v[k];
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0) S.gsum[k][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      double t = 0.0;
+      for (int i = 0; i < NT / 32; ++i) t += S.gsum[threadIdx.x][i];
+      grad[(size_t)3 * (el - 1) + threadIdx.x] += t;
+    }
+    return;
+  }
+  for (int k = threadIdx.x; k < NST; k += NT) {
+    int n, q;
+    double am = 0.0, an = 0.0;
+    if (k < 3 * NEN) {
+      const int i = k / 3;
+      q = k % 3;
+      n = E.nodes[i];
+      for (int gq = 0; gq < NGP; ++gq) {
+        const double gx = G.g[gq][i][0], gy = G.g[gq][i][1], gz = G.g[gq][i][2];
+        if (q == 0) am += gx * S.S6[gq][0] + gy * S.S6[gq][3] + gz * S.S6[gq][5];
+        else if (q == 1) am += gx * S.S6[gq][3] + gy * S.S6[gq][1] + gz * S.S6[gq][4];
+        else am += gx * S.S6[gq][5] + gy * S.S6[gq][4] + gz * S.S6[gq][2];
+      }
+    } else {
+      const int l = k - 3 * NEN;
+      q = 3;
+      n = E.nodes[l];
+      for (int gq = 0; gq < NGP; ++gq) {
+        am -= G.gp[gq][l][0] * S.Q4[gq][1] + G.gp[gq][l][1] * S.Q4[gq][2] +
+              G.gp[gq][l][2] * S.Q4[gq][3];
+        an -= G.hp[gq][l] * S.Q4[gq][0];
+      }
+    }
+    const int e = eq_of(L, n, q);
+    if (e > 0) {
+      mu[e - 1] -= am;
+      if (q == 3) nu[e - 1] -= an;
+    }
+  }
+}
+
 // isw = 5: initial stress, b -= int(B^T sigma0) with sigma0 interpolated by
 // the linear functions from the vertex values (Elmlib03.f:2528-2590).
 template <bool HEXA>
@@ -958,6 +1131,36 @@ cudaError_t launch_rhs4(const ElemLaunch& L, bool hexa, const double* u,
                                   load, fload, maxt, b);
   return launch_elem<SmF<false>>(k_rhs4<false>, L.nelem, 32, s, L, u, dp, eload, eloadp,
                                  load, fload, maxt, b);
+}
+
+// (the shared-memory opt-in is set per kernel: the two modes share a
+// signature, so launch_elem's per-instantiation flag would cover only one)
+template <bool HEXA, int MODE>
+cudaError_t launch_adjoint_t(const ElemLaunch& L, const double* lam, const double* un,
+                             const double* dun, double* mu, double* nu, double* grad,
+                             cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_adjoint<HEXA, MODE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(SmA<HEXA>));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_adjoint<HEXA, MODE><<<L.nelem, ET<HEXA>::NT, sizeof(SmA<HEXA>), s>>>(L, lam, un, dun, mu,
+                                                                          nu, grad);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const ElemLaunch& L, bool hexa, int mode, const double* lam,
+                           const double* un, const double* dun, double* mu, double* nu,
+                           double* grad, cudaStream_t s) {
+  if (L.nelem <= 0) return cudaSuccess;
+  if (hexa)
+    return mode == 0 ? launch_adjoint_t<true, 0>(L, lam, un, dun, mu, nu, grad, s)
+                     : launch_adjoint_t<true, 1>(L, lam, un, dun, mu, nu, grad, s);
+  return mode == 0 ? launch_adjoint_t<false, 0>(L, lam, un, dun, mu, nu, grad, s)
+                   : launch_adjoint_t<false, 1>(L, lam, un, dun, mu, nu, grad, s);
 }
 
 cudaError_t launch_stress5(const ElemLaunch& L, bool hexa, const double* tx0,
