@@ -53,8 +53,14 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one step of the same workload only (for the ncu launch list)")
-    ap.add_argument("--workload", default="cube", choices=["cube", "batched"],
-                    help="batched: only the batch of independent cubes (its own line)")
+    ap.add_argument("--workload", default="cube", choices=["cube", "batched", "adjoint"],
+                    help="batched: only the batch of independent cubes; adjoint: the "
+                         "gradient of a 50-step misfit on a 40^3 cube and its finite-"
+                         "difference check (each its own line)")
+    ap.add_argument("--fd-dirs", type=int, default=2,
+                    help="finite-difference directions of the adjoint workload")
+    ap.add_argument("--adj-n", type=int, default=40)
+    ap.add_argument("--adj-steps", type=int, default=50)
     ap.add_argument("--batch-inst", type=int, default=96)
     ap.add_argument("--batch-steps", type=int, default=2,
                     help="timed steps of the batch leg in the default run")
@@ -324,6 +330,59 @@ def run_batched(args):
               flush=True)
 
 
+def run_adjoint(args):
+    """Adjoint workload: hexa20 cube of --adj-n^3 elements with per-element
+    log E and log k from seeded Gaussian random fields (the heterogeneous
+    cube's), --adj-steps steps of 100 s, misfit of the last step's vertical
+    displacement at 100 seeded top-surface vertex nodes and pressure at 100
+    seeded free-pressure vertex nodes against seeded targets; gradient with
+    respect to (log E, log c_k, log M) of every element by the checkpointed
+    adjoint sweep (checkpoints every round(sqrt(steps)) steps), FP64 solves
+    to 1e-12; checked against central differences (h = 1e-6) along
+    --fd-dirs seeded unit directions."""
+    import torch
+    from poromec_gb300 import adjoint, meshgen
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pb = meshgen.cube_problem(args.adj_n, seed=2024, steps=args.adj_steps)
+    ds, tz, ps, tp = adjoint.sensors_and_targets(pb, n_sensors=100, seed=5)
+    model = adjoint.TimeSteppedMisfit(pb, args.adj_steps, ds, tz, ps, tp, solvtol=1e-12)
+    theta = model.theta0()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = model.forward(theta)
+    t1 = time.perf_counter()
+    g = model.gradient()
+    t2 = time.perf_counter()
+    rng = np.random.default_rng(17)
+    gn = float(np.linalg.norm(g))
+    fd = []
+    h = 1e-6
+    # first the steepest direction g / |g| (directional derivative |g|),
+    # then seeded random unit directions (derivative ~ |g| / sqrt(parameters),
+    # close to the finite-difference noise of the forwards)
+    for k in range(args.fd_dirs):
+        d = g / gn if k == 0 else rng.standard_normal(theta.shape)
+        d = d / np.linalg.norm(d)
+        f = (model.forward(theta + h * d, False) - model.forward(theta - h * d, False)) / (2 * h)
+        a = float(np.sum(g * d))
+        fd.append({"direction": "gradient" if k == 0 else "random", "fd": f, "adjoint": a,
+                   "abs_err_over_grad_norm": abs(f - a) / gn,
+                   "rel_err": abs(f - a) / max(abs(f), 1e-300)})
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "adjoint gradient of a time-stepped Biot misfit", "workload":
+        "hexa20 %d^3 cube, %d steps, per-element log E, log k, log M" % (args.adj_n,
+                                                                        args.adj_steps),
+        "value": (t2 - t0), "unit": "s per gradient (forward + reverse)",
+        "higher_is_better": False, "forward_s": t1 - t0, "reverse_s": t2 - t1,
+        "parameters": int(3 * pb["numel"]), "equations": int(model.m.neq), "J": J,
+        "grad_norm": gn, "checkpoint_every": model.ckpt, "solves": model.solves,
+        "fd_step": h, "fd_checks": fd, "data": "synthetic (seeded fields and targets)"}),
+        flush=True)
+
+
 def run_gpu(args):
     import torch
     rank, world, local = dist_env()
@@ -515,6 +574,8 @@ def main():
         run_spmv_only(args)
     elif args.workload == "batched" and args.impl != "reference":
         run_batched(args)
+    elif args.workload == "adjoint" and args.impl != "reference":
+        run_adjoint(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
