@@ -288,8 +288,13 @@ def batched_leg(args, steps, warmup):
     import torch
     import poromec_gb300 as pg
     from poromec_gb300 import meshgen
+    rank, world, _ = dist_env()
     t0 = time.perf_counter()
-    inst = meshgen.batch_instances(ninst=args.batch_inst, nmin=8, nmax=32, seed=4242)
+    allinst = meshgen.batch_instances(ninst=args.batch_inst, nmin=8, nmax=32, seed=4242)
+    # N > 1: each rank steps its share of the instances (weak scaling, no
+    # exchange in the solve); the time is the slowest rank's
+    share = meshgen.partition_instances([p["n"] for p in allinst], world)[rank]
+    inst = [allinst[i] for i in share]
     pb = meshgen.union_problem(inst)
     m = pg.from_problem(pb)
     m.set_precision(pg.capi.PM_FP32C_REFINE)
@@ -306,10 +311,15 @@ def batched_leg(args, steps, warmup):
         its.append(m.batch_iters()[0].copy())
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([el], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        el = float(t.item())
     it = np.array(its)
     ns = np.array([p["n"] for p in inst])
-    out = {"value": len(inst) * steps / el, "unit": "instance-steps/s",
-           "ms_per_step": el / steps * 1e3, "instances": len(inst), "steps": steps,
+    out = {"value": len(allinst) * steps / el, "unit": "instance-steps/s",
+           "ranks": world, "instances_this_rank": len(inst),
+           "ms_per_step": el / steps * 1e3, "instances": len(allinst), "steps": steps,
            "warmup": warmup, "equations": int(m.neq), "nad": int(m.nad),
            "edge_min": int(ns.min()), "edge_max": int(ns.max()),
            "pcg_iterations_max": int(it.max()), "pcg_iterations_mean": float(it.mean()),
@@ -324,6 +334,8 @@ def run_batched(args):
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
     b = batched_leg(args, args.steps, args.warmup)
     if rank == 0:
         print(json.dumps(dict(metric="batched Biot steps", workload="batched cubes", **b)),

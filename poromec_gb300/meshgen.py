@@ -363,3 +363,17 @@ def union_problem(instances):
               maxit=first.get("maxit"), maxnlit=first.get("maxnlit"),
               name="batch of %d instances" % len(instances))
     return pb
+
+
+def partition_instances(edges, world):
+    """Instances of a batch split over world ranks, balanced by estimated
+    work (nonzeros grow as n^3 for an n^3 cube): largest first, each to the
+    rank with the least work so far.  Returns one sorted index list per rank;
+    the ranks solve their shares independently (no exchange in the solve)."""
+    load = [0.0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(edges)), key=lambda k: (-int(edges[k]) ** 3, k)):
+        r = min(range(world), key=lambda j: (load[j], j))
+        parts[r].append(i)
+        load[r] += float(edges[i]) ** 3
+    return [sorted(p) for p in parts]
