@@ -140,6 +140,8 @@ struct Handle {
   int numcolors = 0;
   int precision = PM_FP64;
   double inner_tol = 1.0e-5;   // inner tolerance of the FP32 refinement sweeps
+                               // (and of a compensated MINRES cycle)
+  double cycle_conv = 0.0;     // the current compensated MINRES cycle's target
   bool debug = false;          // PM_DEBUG set: solver progress on stderr
   std::vector<int32_t> color_ptr;
   std::vector<int32_t> h_eq;       // (ndf, nnode)

@@ -537,6 +537,69 @@ __device__ __forceinline__ void f2_fma(F2& acc, float vh, int q, float xh, float
   acc.c += c;
 }
 
+// Packed two-lane FP32 arithmetic of sm_100+ (fma/add/sub/mul .rn.f32x2):
+// two rows of a node, which share the column's x pair, in one instruction.
+// Each lane is an IEEE round-to-nearest FP32 operation, so the error-free
+// transformations below hold lane by lane.
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x pk2(float a, float b) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 up2(f2x r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+  f2x d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2x add2(f2x a, f2x b) {
+  f2x d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x sub2(f2x a, f2x b) {
+  f2x d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+  f2x d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// Compensated accumulation of two rows at once.  sn holds minus the running
+// sum of the rounded products t (so that the product can be formed as
+// tn = hi * (-xh) = -t and its error as fma(hi, xh, tn) without negations),
+// cn minus the TwoSum errors, cp the product corrections
+// e + hi*xl + t*q*2^-31; the row value is -sn + (cp - cn).
+struct P2 {
+  f2x sn, cn, cp;
+};
+
+__device__ __forceinline__ void p2_fma(P2& a, f2x vh, f2x nqs, f2x xh, f2x nxh, f2x xl) {
+  const f2x tn = mul2(vh, nxh);
+  const f2x e = fma2(vh, xh, tn);
+  const f2x s = add2(a.sn, tn);
+  const f2x bp = sub2(s, a.sn);
+  const f2x err = add2(sub2(a.sn, sub2(s, bp)), sub2(tn, bp));
+  a.sn = s;
+  a.cn = add2(a.cn, err);
+  a.cp = fma2(vh, xl, fma2(tn, nqs, add2(a.cp, e)));
+}
+
+// -q0 2^-31, -q1 2^-31 for two int8 corrections (the magic-number
+// conversion of q_scale, with the sign folded into the constants)
+__device__ __forceinline__ f2x p2_nqs(int q0, int q1) {
+  const f2x f = pk2(__int_as_float(0x4B400000 + q0), __int_as_float(0x4B400000 + q1));
+  return fma2(f, pk2(-0x1p-31f, -0x1p-31f), pk2(0x1.8p-8f, 0x1.8p-8f));
+}
+
 __device__ __forceinline__ F2 f2_shfl(F2 a, int m) {
   return F2{__shfl_xor_sync(0xffffffffu, a.s, m), __shfl_xor_sync(0xffffffffu, a.c, m)};
 }
@@ -548,12 +611,14 @@ __device__ __forceinline__ F2 f2_shfl(F2 a, int m) {
 // a dependent index load.  Values and column indices are read once per
 // product and loaded with the evict-first hint, which leaves L2 to the
 // gathered operand.  The last trip is masked.
-template <int D, int S, int U>
+template <int D, int S, int U, bool PK>
 __device__ __forceinline__ void cf_rows(const float* __restrict__ h,
                                         const int8_t* __restrict__ l,
                                         const int32_t* __restrict__ cols,
                                         const float2* __restrict__ xp, int W, int t,
                                         F2 (&a)[4]) {
+  // PK: rows 2k, 2k+1 in packed two-lane arithmetic (an odd last row scalar)
+  P2 pa[2] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
   int cn[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) cn[u] = (t + u * S < W) ? __ldcs(&cols[t + u * S]) : -1;
@@ -575,11 +640,32 @@ __device__ __forceinline__ void cf_rows(const float* __restrict__ h,
 #pragma unroll
     for (int u = 0; u < U; ++u)
       cn[u] = (cnext + u * S < W) ? __ldcs(&cols[cnext + u * S]) : -1;
+    if (PK) {
 #pragma unroll
-    for (int u = 0; u < U; ++u)
+      for (int u = 0; u < U; ++u) {
+        const f2x xh = pk2(xv[u].x, xv[u].x), nxh = pk2(-xv[u].x, -xv[u].x);
+        const f2x xl = pk2(xv[u].y, xv[u].y);
 #pragma unroll
-      for (int r = 0; r < D; ++r)
-        f2_fma(a[r], hv[u][r], lv[u][r], xv[u].x, xv[u].y);
+        for (int k = 0; k < D / 2; ++k)
+          p2_fma(pa[k], pk2(hv[u][2 * k], hv[u][2 * k + 1]),
+                 p2_nqs(lv[u][2 * k], lv[u][2 * k + 1]), xh, nxh, xl);
+        if (D & 1) f2_fma(a[D - 1], hv[u][D - 1], lv[u][D - 1], xv[u].x, xv[u].y);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+          f2_fma(a[r], hv[u][r], lv[u][r], xv[u].x, xv[u].y);
+    }
+  }
+  if (PK) {
+#pragma unroll
+    for (int k = 0; k < D / 2; ++k) {
+      const float2 sn = up2(pa[k].sn), cn2 = up2(pa[k].cn), cp = up2(pa[k].cp);
+      a[2 * k] = F2{-sn.x, cp.x - cn2.x};
+      a[2 * k + 1] = F2{-sn.y, cp.y - cn2.y};
+    }
   }
 }
 
@@ -589,7 +675,7 @@ __device__ __forceinline__ void cf_rows(const float* __restrict__ h,
 // chosen per matrix by the autotuner.  With S = 32 a warp reads each panel
 // row as full 128-byte lines; with S = 8 four nodes share a warp and each
 // load instruction touches four lines.
-template <int MODE, int S, int U>
+template <int MODE, int S, int U, bool PK>
 __global__ void __launch_bounds__(256)
     k_spmv_cf(PanelView P, const float* __restrict__ vh, const int8_t* __restrict__ vl,
               const float2* __restrict__ xp, double* __restrict__ y, const double* __restrict__ xd,
@@ -615,10 +701,10 @@ __global__ void __launch_bounds__(256)
       const float* h = vh + vo;
       const int8_t* l = vl + vo;
       const int32_t* cols = P.cols + P.col_off[node];
-      if (d == 4) cf_rows<4, S, U>(h, l, cols, xp, W, t, a);
-      else if (d == 3) cf_rows<3, S, U>(h, l, cols, xp, W, t, a);
-      else if (d == 2) cf_rows<2, S, U>(h, l, cols, xp, W, t, a);
-      else cf_rows<1, S, U>(h, l, cols, xp, W, t, a);
+      if (d == 4) cf_rows<4, S, U, PK>(h, l, cols, xp, W, t, a);
+      else if (d == 3) cf_rows<3, S, U, PK>(h, l, cols, xp, W, t, a);
+      else if (d == 2) cf_rows<2, S, U, PK>(h, l, cols, xp, W, t, a);
+      else cf_rows<1, S, U, PK>(h, l, cols, xp, W, t, a);
     }
     // transposed butterfly on (sum, correction) pairs over the S lanes: the
     // first two levels halve the rows each lane carries, the rest add
@@ -1221,11 +1307,11 @@ int resident_grid(K kernel) {
   return g < kRedBlocks ? g : kRedBlocks;
 }
 
-template <int MODE, int S, int U>
+template <int MODE, int S, int U, bool PK = false>
 void launch_cf(const PanelView& P, CompVals C, const float2* xp, double* y, const double* xd,
                KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s) {
-  static const int grid = resident_grid(k_spmv_cf<MODE, S, U>);
-  k_spmv_cf<MODE, S, U><<<grid, 256, 0, s>>>(
+  static const int grid = resident_grid(k_spmv_cf<MODE, S, U, PK>);
+  k_spmv_cf<MODE, S, U, PK><<<grid, 256, 0, s>>>(
       P, C.hi, C.lo, xp, y, xd, ks, partial, counter);
 }
 
@@ -1280,6 +1366,10 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
     case 21: launch_cf<MODE, 32, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 22: launch_cf<MODE, 32, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 24: launch_cf<MODE, 32, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 104: launch_cf<MODE, 8, 4, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 112: launch_cf<MODE, 16, 2, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 114: launch_cf<MODE, 16, 4, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 124: launch_cf<MODE, 32, 4, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
     default: launch_cf<MODE, 8, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
   }
 }
