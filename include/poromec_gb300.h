@@ -145,9 +145,12 @@ int pm_assemble(pm_handle h, int isw, int lhs, int rhs, const double* u, double*
 int pm_spmv(pm_handle h, const double* x, double* y);
 
 /* solv_pm (Solv.f:27-780): solver 1 = PCG (Iters.f:299-595),
- * 7 = preconditioned MINRES (Iters.f:3987-4305, 10 restarts);
- * precond 2 = diag 1/ad, 5 = |1/ad| (Precond.f:22-79).  x is set to 0 first
- * (fnew = .true.).  b, x host arrays of length neq. */
+ * 7 = preconditioned MINRES (Iters.f:3987-4305, 10 restarts),
+ * 11 = rpsqmr (Iters.f:6100-6439, the reference's default; FP64 only; where
+ * it does not converge in maxit the reference switches to GMRES(l), here the
+ * call returns PM_E_NOCONV); precond 2 = diag 1/ad, 5 = |1/ad|
+ * (Precond.f:22-79).  x is set to 0 first (fnew = .true.).  b, x host arrays
+ * of length neq. */
 int pm_solve(pm_handle h, int solver, int precond, const double* b, double* x,
              double tol, int maxit, pm_step_info* info);
 

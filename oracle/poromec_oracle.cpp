@@ -1588,6 +1588,70 @@ int or_pform_range(or_handle h, int isw, int lhs, int rhs, const double* u,
   return pform(h, isw, lhs != 0, rhs != 0, u, b, nthreads, nullptr, e_begin, e_end, false);
 }
 
+// rpsqmr (Iters.f:6100-6439): symmetric QMR with the diagonal
+// preconditioner applied on the right, for symmetric indefinite systems.
+// conv = tol ||b||; the loop stops when ||r|| < conv; a non-converged run
+// returns OR_E_NOCONV (where the reference sets fsqmr and switches to
+// GMRES(l), Solv.f:707-766); sigma = 0 or rho = 0 are breakdowns
+// (stop_mef in the reference).
+int rpsqmr(or_handle_s* h, const double* m, const double* b, double* x, double tol,
+           int maxit, int nth, or_step_info* info) {
+  const int neq = h->neq;
+  for (int i = 0; i < neq; ++i)
+    if (h->ad[i] == 0.0) return OR_E_ZERO_DIAG;
+  std::vector<double> t(neq), r(neq), q(neq), d(neq);
+  for (int i = 0; i < neq; ++i) x[i] = 0.0;
+  const double norm_b = dot(b, b, neq, nth);
+  const double conv = tol * std::sqrt(std::fabs(norm_b));
+  matvec(h, x, t.data(), nth);
+  for (int i = 0; i < neq; ++i) {
+    r[i] = b[i] - t[i];
+    q[i] = r[i] * m[i];
+    d[i] = 0.0;
+  }
+  double tau = std::sqrt(dot(r.data(), r.data(), neq, nth));
+  double ro = dot(r.data(), q.data(), neq, nth);
+  double v0 = 0.0;
+  int j;
+  bool converged = false;
+  for (j = 1; j <= maxit; ++j) {
+    matvec(h, q.data(), t.data(), nth);
+    const double sigma = dot(q.data(), t.data(), neq, nth);
+    if (sigma == 0.0) return OR_E_NOCONV;
+    const double alpha = ro / sigma;
+    for (int i = 0; i < neq; ++i) r[i] = r[i] - alpha * t[i];
+    const double vn = std::sqrt(dot(r.data(), r.data(), neq, nth)) / tau;
+    const double cn = 1.0 / std::sqrt(1.0 + vn * vn);
+    tau = tau * vn * cn;
+    const double tmp1 = cn * cn * v0 * v0;
+    const double tmp2 = cn * cn * alpha;
+    for (int i = 0; i < neq; ++i) {
+      d[i] = tmp1 * d[i] + tmp2 * q[i];
+      x[i] = x[i] + d[i];
+      t[i] = r[i] * m[i];
+    }
+    v0 = vn;
+    if (ro == 0.0) return OR_E_NOCONV;
+    const double rt = dot(r.data(), t.data(), neq, nth);
+    const double beta = rt / ro;
+    ro = rt;
+    for (int i = 0; i < neq; ++i) q[i] = t[i] + beta * q[i];
+    const double norm_r = std::sqrt(dot(r.data(), r.data(), neq, nth));
+    if (norm_r < conv) {
+      converged = true;
+      break;
+    }
+  }
+  if (info) {
+    info->iters = converged ? j : maxit;
+    info->conv = conv;
+  }
+  if (!converged) return OR_E_NOCONV;
+  matvec(h, x, t.data(), nth);
+  if (info) info->xkx = dot(x, t.data(), neq, nth);
+  return OR_OK;
+}
+
 int or_matvec(or_handle h, const double* x, double* y, int nthreads) {
   if (!h || !x || !y) return OR_E_ARG;
   matvec(h, x, y, nthreads);
@@ -1606,6 +1670,7 @@ int or_solve(or_handle h, int solver, int precond, const double* b, double* x,
   }
   if (solver == 1) return pcg(h, h->m.data(), b, x, tol, maxit, nthreads, info);
   if (solver == 7) return pminres(h, h->m.data(), b, x, tol, maxit, nthreads, info);
+  if (solver == 11) return rpsqmr(h, h->m.data(), b, x, tol, maxit, nthreads, info);
   return OR_E_ARG;
 }
 

@@ -91,7 +91,9 @@ int or_pform_range(or_handle h, int isw, int lhs, int rhs, const double* u,
 int or_matvec(or_handle h, const double* x, double* y, int nthreads);
 
 /* solv_pm (Solv.f:27-780): solver 1 = pcg (Iters.f:299-595), 7 = pminres
- * (Iters.f:3987-4305, 10 restarts); precond 2 = 1/ad, 5 = |1/ad|
+ * (Iters.f:3987-4305, 10 restarts), 11 = rpsqmr (Iters.f:6100-6439; no
+ * convergence returns OR_E_NOCONV where the reference switches to GMRES(l));
+ * precond 2 = 1/ad, 5 = |1/ad|
  * (Precond.f:22-79).  x is zeroed first (fnew = .true.). */
 int or_solve(or_handle h, int solver, int precond, const double* b, double* x,
              double tol, int maxit, int nthreads, or_step_info* info);

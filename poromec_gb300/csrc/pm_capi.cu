@@ -451,8 +451,37 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       }
       --nrestart;
     }
+  } else if (solver == 11) {
+    if (comp) {
+      h->err = "rpsqmr (solver 11) runs on the FP64 operator (PM_FP64)";
+      return PM_E_ARG;
+    }
+    if (!h->sqmr_graph) {
+      PM_TRY(capture(h, &h->sqmr_graph, [&]() {
+        return pm::sqmr_iteration(P, val64, n, h->D.m, V, h->D.ks, h->D.partial, h->D.counter,
+                                  h->stream);
+      }));
+    }
+    h->launches += 1;
+    PM_CUDA(pm::sqmr_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
+                          h->stream));
+    for (;;) {
+      PM_CUDA(cudaGraphLaunch(h->sqmr_graph, h->stream));
+      h->launches += 4 * kGraphIters;
+      PM_TRY(read_scalars(h, &ks));
+      if (ks.conv_flag) break;
+    }
+    if (ks.conv_flag != 1) {
+      h->err = ks.conv_flag == 3
+                   ? "rpsqmr: breakdown (sigma or rho zero, or non-finite) after " +
+                         std::to_string(ks.iter) + " iterations"
+                   : "rpsqmr: no convergence reached after " + std::to_string(ks.iter) +
+                         " iterations (the reference switches to GMRES(l) here)";
+      if (info) info->iters = ks.iter;
+      return PM_E_NOCONV;
+    }
   } else {
-    h->err = "solver must be 1 (pcg) or 7 (minres)";
+    h->err = "solver must be 1 (pcg), 7 (minres) or 11 (rpsqmr)";
     return PM_E_ARG;
   }
   PM_CUDA(cudaEventRecord(e1, h->stream));
@@ -951,6 +980,7 @@ void free_all(Handle* h) {
   if (h->pcgm_graph) cudaGraphExecDestroy(h->pcgm_graph);
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
   if (h->pcgc_graph) cudaGraphExecDestroy(h->pcgc_graph);
+  if (h->sqmr_graph) cudaGraphExecDestroy(h->sqmr_graph);
   if (h->bpcg_graph) cudaGraphExecDestroy(h->bpcg_graph);
   if (h->bpcgc_graph) cudaGraphExecDestroy(h->bpcgc_graph);
   for (void* p : {(void*)h->B.eq_ptr, (void*)h->B.blk_ptr, (void*)h->B.blk_inst, (void*)h->B.bs,

@@ -186,6 +186,7 @@ struct Handle {
   cudaGraphExec_t pcg_graph = nullptr, minres_graph = nullptr, pcgm_graph = nullptr;
   cudaGraphExec_t pcgc_graph = nullptr, minresc_graph = nullptr;
   cudaGraphExec_t bpcg_graph = nullptr, bpcgc_graph = nullptr;
+  cudaGraphExec_t sqmr_graph = nullptr;
   double timers[8] = {0};
   int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;

@@ -69,6 +69,13 @@ cudaError_t pcg_init(int n, const double* b, const double* m, KrylovVecs& V,
 cudaError_t pcg_iteration(const PanelView& P, const double* val64, int n, const double* m,
                           KrylovVecs& V, KrylovScalars* ks, double* partial,
                           unsigned* counter, cudaStream_t s);
+// rpsqmr (Iters.f:6100-6439): init and one iteration (4 launches)
+cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V,
+                      KrylovScalars* ks, double tol, int maxit, double* partial,
+                      unsigned* counter, cudaStream_t s);
+cudaError_t sqmr_iteration(const PanelView& P, const double* val64, int n, const double* m,
+                           KrylovVecs& V, KrylovScalars* ks, double* partial,
+                           unsigned* counter, cudaStream_t s);
 cudaError_t minres_conv(int n, const double* b, const double* m, KrylovScalars* ks,
                         double tol, double* partial, unsigned* counter, cudaStream_t s);
 // pair != nullptr also writes the FP32 pair of z0 (compensated iteration)

