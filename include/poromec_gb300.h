@@ -202,6 +202,17 @@ int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* d_ja,
  * The first compensated solve or product runs it implicitly. */
 int pm_tune_spmv(pm_handle h, int* shape);
 
+/* tform_pm (Pform.f:433-640) with the element stress pass isw 3
+ * (Elmlib03.f:2206-2256 hexa20, 440-495 tetra10) and effective_stress
+ * (Pform.f:2487-2505): from the current state, per node (6, nnode) the total
+ * stress, the Biot effective stress (total + alpha p) and the effective stress
+ * (total + p), and (3, nnode) the Darcy flux; vertex nodes average the values
+ * of the elements that share them, mid-side nodes are zero.  The '_dev' form
+ * takes device arrays (stream as pm_spmv_dev). */
+int pm_stress(pm_handle h, double* tx, double* txb, double* txe, double* flux);
+int pm_stress_dev(pm_handle h, double* d_tx, double* d_txb, double* d_txe, double* d_flux,
+                  void* stream);
+
 /* Material table (e, PM_PROP per material) replaced, same numat as at
  * creation; the next step re-assembles.  With one material per element
  * (numat = numel) this sets per-element parameters. */

@@ -135,6 +135,14 @@ class Oracle:
         _check(lib().or_get_state(self.h, _p(u), _p(u0), _p(dp)), "or_get_state")
         return u, u0, dp
 
+    def stress(self):
+        """tform_pm isw 3 + effective_stress: total, Biot and effective stress
+        (nnode, 6) and Darcy flux (nnode, 3) of the current state."""
+        tx, txb, txe = np.zeros((self.nnode, 6)), np.zeros((self.nnode, 6)), np.zeros((self.nnode, 6))
+        fl = np.zeros((self.nnode, 3))
+        _check(lib().or_stress(self.h, _p(tx), _p(txb), _p(txe), _p(fl)), "or_stress")
+        return tx, txb, txe, fl
+
     def get_id(self):
         idr = np.zeros((self.nnode, 4), np.int32)
         _check(lib().or_get_id(self.h, _p(idr)), "or_get_id")

@@ -893,6 +893,70 @@ void element(bool hexa, const double* e, const int* iqm, const int* iqh,
       rhs_gp(p, nu, np, hu, hux, huy, huz, hp, hpx, hpy, hpz, u, dp, w, m, env);
     }
     face_loads(p, hexa, iqm, iqh, x, L, env);
+  } else if (isw == 3) {
+    // stresses and fluxes at the vertices (Elmlib03.f:2206-2256 hexa20,
+    // :440-495 tetra10): p(6 i ..) total stress D eps - alpha dp, then
+    // p(6 np + 6 i ..) the Biot effective stress (total + alpha p), then
+    // p(12 np + 3 i ..) the Darcy flux perm (rho_f g - grad p)
+    static const double RNH[8] = {1, -1, -1, 1, 1, -1, -1, 1};
+    static const double SNH[8] = {1, 1, -1, -1, 1, 1, -1, -1};
+    static const double TNH[8] = {1, 1, 1, 1, -1, -1, -1, -1};
+    static const double RNT[4] = {1, 0, 0, 0}, SNT[4] = {0, 1, 0, 0}, TNT[4] = {0, 0, 1, 0};
+    for (int i = 0; i < np; ++i) {
+      const double ri = hexa ? RNH[i] : RNT[i], si = hexa ? SNH[i] : SNT[i],
+                   ti = hexa ? TNH[i] : TNT[i];
+      if (hexa) {
+        sfhexa8_m(hp, hpx, hpy, hpz, ri, si, ti, false, true);
+        jacob3d_m(hpx, hpy, hpz, xj, xji, x, det, 8, true);
+        sfhexa20_m(hu, hux, huy, huz, ri, si, ti, false, true);
+        jacob3d_m(hux, huy, huz, xj, xji, x, det, 20, false);
+      } else {
+        sftetra4(hp, hpx, hpy, hpz, ri, si, ti, false, true);
+        jacob3d_m(hpx, hpy, hpz, xj, xji, x, det, 4, true);
+        sftetra10(hu, hux, huy, huz, ri, si, ti, false, true);
+        jacob3d_m(hux, huy, huz, xj, xji, x, det, 10, false);
+      }
+      double epsi[6];
+      double* t = p + 6 * i;
+      double* tb = p + 6 * np + 6 * i;
+      deform3d(hux, huy, huz, u, epsi, nu);
+      stress3d(m.a, m.b, m.c, epsi, t);
+      const double dpm = m.coef_biot * dp[i];
+      const double pm = m.coef_biot * u[3 * nu + i];
+      t[0] = t[0] - dpm;
+      t[1] = t[1] - dpm;
+      t[2] = t[2] - dpm;
+      tb[0] = t[0] + pm;
+      tb[1] = t[1] + pm;
+      tb[2] = t[2] + pm;
+      tb[3] = t[3];
+      tb[4] = t[4];
+      tb[5] = t[5];
+    }
+    for (int i = 0; i < np; ++i) {
+      const double ri = hexa ? RNH[i] : RNT[i], si = hexa ? SNH[i] : SNT[i],
+                   ti = hexa ? TNH[i] : TNT[i];
+      if (hexa) {
+        sfhexa8_m(hp, hpx, hpy, hpz, ri, si, ti, true, true);
+        jacob3d_m(hpx, hpy, hpz, xj, xji, x, det, 8, true);
+      } else {
+        sftetra4(hp, hpx, hpy, hpz, ri, si, ti, true, true);
+        jacob3d_m(hpx, hpy, hpz, xj, xji, x, det, 4, true);
+      }
+      // darcy_flux (Elmlib.f:3178-3200)
+      double* q = p + 12 * np + 3 * i;
+      q[0] = m.fluid_d * env.gravity[0];
+      q[1] = m.fluid_d * env.gravity[1];
+      q[2] = m.fluid_d * env.gravity[2];
+      for (int k = 0; k < np; ++k) {
+        q[0] = q[0] - hpx[k] * u[3 * nu + k];
+        q[1] = q[1] - hpy[k] * u[3 * nu + k];
+        q[2] = q[2] - hpz[k] * u[3 * nu + k];
+      }
+      q[0] = m.perm * q[0];
+      q[1] = m.perm * q[1];
+      q[2] = m.perm * q[2];
+    }
   } else if (isw == 5) {
     for (int g = 0; g < ngp; ++g) {
       double ri, si, ti, wq, w;
@@ -1570,6 +1634,60 @@ int or_element(or_handle h, int nel, int isw, const double* ul,
             s, txn, isw, h->L, h->env);
   } catch (DetError&) {
     return OR_E_DET;
+  }
+  return OR_OK;
+}
+
+// tform_pm (Pform.f:433-640) with isw 3, then effective_stress
+// (Pform.f:2487-2505): vertex values of every element accumulated in element
+// order and averaged over the elements sharing the vertex; mid-side nodes
+// keep zeros.  tx, txb, txe (6, nnode), flux (3, nnode), from the current u
+// and dp.
+int or_stress(or_handle h, double* tx, double* txb, double* txe, double* flux) {
+  if (!h || !tx || !txb || !txe || !flux) return OR_E_ARG;
+  const int nnode = h->nnode, nenv = h->nenv, nen = h->nen;
+  std::vector<int> ic(nnode, 0);
+  std::fill(tx, tx + (size_t)6 * nnode, 0.0);
+  std::fill(txb, txb + (size_t)6 * nnode, 0.0);
+  std::fill(flux, flux + (size_t)3 * nnode, 0.0);
+  int ld[68], iqm[7], iqh[7];
+  double ul[68], xl[24], dpl[8], txn[48], pl[120], sdum[1];
+  for (int nel = 1; nel <= h->numel; ++nel) {
+    gather_element(h, nel, h->u.data(), ld, ul, xl, dpl, iqm, iqh, txn, nullptr);
+    const int ma = h->ix[(size_t)(nen + 1) * (nel - 1) + nen];
+    for (int i = 0; i < 15 * nenv; ++i) pl[i] = 0.0;
+    try {
+      element(h->hexa, &h->e[(size_t)OR_PROP * (ma - 1)], iqm, iqh, xl, ul, dpl, pl, sdum,
+              txn, 3, h->L, h->env);
+    } catch (DetError&) {
+      return OR_E_DET;
+    }
+    for (int i = 0; i < nenv; ++i) {
+      const int no = h->ix[(size_t)(nen + 1) * (nel - 1) + i];
+      if (no <= 0) continue;
+      ic[no - 1] += 1;
+      for (int j = 0; j < 6; ++j) {
+        tx[(size_t)6 * (no - 1) + j] += pl[6 * i + j];
+        txb[(size_t)6 * (no - 1) + j] += pl[6 * nenv + 6 * i + j];
+      }
+      for (int j = 0; j < 3; ++j) flux[(size_t)3 * (no - 1) + j] += pl[12 * nenv + 3 * i + j];
+    }
+  }
+  for (int i = 0; i < nnode; ++i) {
+    if (h->fnno[i] == 1 && ic[i] > 0) {
+      for (int j = 0; j < 6; ++j) {
+        tx[(size_t)6 * i + j] = tx[(size_t)6 * i + j] / ic[i];
+        txb[(size_t)6 * i + j] = txb[(size_t)6 * i + j] / ic[i];
+      }
+      for (int j = 0; j < 3; ++j) flux[(size_t)3 * i + j] = flux[(size_t)3 * i + j] / ic[i];
+    }
+  }
+  for (int i = 0; i < nnode; ++i) {
+    const double pi = h->u[(size_t)h->ndf * i + h->ndf - 1];
+    txe[(size_t)6 * i + 0] = tx[(size_t)6 * i + 0] + pi;
+    txe[(size_t)6 * i + 1] = tx[(size_t)6 * i + 1] + pi;
+    txe[(size_t)6 * i + 2] = tx[(size_t)6 * i + 2] + pi;
+    for (int j = 3; j < 6; ++j) txe[(size_t)6 * i + j] = tx[(size_t)6 * i + j];
   }
   return OR_OK;
 }

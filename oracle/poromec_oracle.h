@@ -90,6 +90,12 @@ int or_pform_range(or_handle h, int isw, int lhs, int rhs, const double* u,
  * row-partitioned variant with per-thread buffers (Matvec_omp.f:461-587). */
 int or_matvec(or_handle h, const double* x, double* y, int nthreads);
 
+/* tform_pm (Pform.f:433-640, element isw 3: Elmlib03.f:2206-2256 /
+ * 440-495) and effective_stress (Pform.f:2487-2505): nodal total, Biot and
+ * effective stress (6 per node) and Darcy flux (3 per node) at the vertices
+ * from the current u and dp; mid-side nodes zero. */
+int or_stress(or_handle h, double* tx, double* txb, double* txe, double* flux);
+
 /* solv_pm (Solv.f:27-780): solver 1 = pcg (Iters.f:299-595), 7 = pminres
  * (Iters.f:3987-4305, 10 restarts), 11 = rpsqmr (Iters.f:6100-6439; no
  * convergence returns OR_E_NOCONV where the reference switches to GMRES(l));

@@ -86,6 +86,8 @@ def load(path=None):
     lib.pm_matvec_csrd_dev.argtypes = [c_i, c_p, c_p, c_p, c_p, c_p, c_p, c_p]
     lib.pm_get_timers.argtypes = [c_p, c_p, c_i]
     lib.pm_set_materials.argtypes = [c_p, c_p, c_i]
+    lib.pm_stress.argtypes = [c_p] * 5
+    lib.pm_stress_dev.argtypes = [c_p] * 6
     lib.pm_adjoint_apply_dev.argtypes = [c_p] * 5
     lib.pm_adjoint_grad_dev.argtypes = [c_p] * 6
     _lib = lib
@@ -196,6 +198,22 @@ class Mesh:
 
     def set_refine(self, inner_tol=1e-5):
         self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
+
+    def stress(self):
+        """tform_pm isw 3 + effective_stress of the current state: total, Biot
+        and effective stress (nnode, 6), Darcy flux (nnode, 3)."""
+        tx, txb, txe = np.zeros((self.nnode, 6)), np.zeros((self.nnode, 6)), np.zeros((self.nnode, 6))
+        fl = np.zeros((self.nnode, 3))
+        self._check(self.lib.pm_stress(self.h, _p(tx), _p(txb), _p(txe), _p(fl)), "pm_stress")
+        return tx, txb, txe, fl
+
+    def stress_dev(self, tx_ptr, txb_ptr, txe_ptr, flux_ptr, stream=None):
+        """stress() into device arrays (6, 6, 6, 3 doubles per node)."""
+        self._check(self.lib.pm_stress_dev(self.h, ctypes.c_void_p(tx_ptr),
+                                           ctypes.c_void_p(txb_ptr), ctypes.c_void_p(txe_ptr),
+                                           ctypes.c_void_p(flux_ptr),
+                                           ctypes.c_void_p(stream) if stream else None),
+                    "pm_stress_dev")
 
     def set_materials(self, e):
         """Replace the material table (numat rows of PM_PROP values)."""

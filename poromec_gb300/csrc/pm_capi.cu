@@ -121,6 +121,27 @@ __global__ void k_delta_update(int nnode, const int32_t* __restrict__ eq,
   }
 }
 
+// tform_pm's average over the elements that share a vertex node (mid-side
+// nodes keep zeros) and effective_stress (Pform.f:2487-2505): txe = tx + p
+// on the normal components
+__global__ void k_stress_finish(int nnode, const int32_t* __restrict__ fnno,
+                                const int* __restrict__ cnt, const double* __restrict__ u,
+                                double* __restrict__ tx, double* __restrict__ txb,
+                                double* __restrict__ txe, double* __restrict__ flux) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
+    if (fnno[i] == 1 && cnt[i] > 0) {
+      const double c = (double)cnt[i];
+      for (int j = 0; j < 6; ++j) {
+        tx[6 * (size_t)i + j] = tx[6 * (size_t)i + j] / c;
+        txb[6 * (size_t)i + j] = txb[6 * (size_t)i + j] / c;
+      }
+      for (int j = 0; j < 3; ++j) flux[3 * (size_t)i + j] = flux[3 * (size_t)i + j] / c;
+    }
+    const double p = u[4 * (size_t)i + 3];
+    for (int j = 0; j < 6; ++j) txe[6 * (size_t)i + j] = tx[6 * (size_t)i + j] + (j < 3 ? p : 0.0);
+  }
+}
+
 // equation-space vector -> nodal layout (4 per node), zero on restrained dofs
 __global__ void k_eq_to_nodal(int nnode, const int32_t* __restrict__ eq,
                               const double* __restrict__ v, double* __restrict__ out) {
@@ -1655,6 +1676,51 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   h->timers[7] = (double)(h->launches - launches0);
   if (info) *info = loc;
   return PM_OK;
+}
+
+int pm_stress_dev(pm_handle hh, double* d_tx, double* d_txb, double* d_txe, double* d_flux,
+                  void* stream) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !d_tx || !d_txb || !d_txe || !d_flux) return PM_E_ARG;
+  cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+  // the state and the scratch belong to the handle's stream
+  if (stream) PM_CUDA(cudaStreamSynchronize(h->stream));
+  const size_t nn = (size_t)h->nnode;
+  int* cnt = reinterpret_cast<int*>(h->D.bx);  // scratch: nnode doubles hold nnode ints
+  PM_CUDA(cudaMemsetAsync(d_tx, 0, sizeof(double) * 6 * nn, s));
+  PM_CUDA(cudaMemsetAsync(d_txb, 0, sizeof(double) * 6 * nn, s));
+  PM_CUDA(cudaMemsetAsync(d_flux, 0, sizeof(double) * 3 * nn, s));
+  PM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * nn, s));
+  h->launches += h->numcolors + 1;
+  for (int c = 0; c < h->numcolors; ++c)
+    PM_CUDA(pm::launch_stress3(elem_launch(h, c), h->hexa, h->D.u, h->D.dp, d_tx, d_txb, d_flux,
+                               cnt, s));
+  k_stress_finish<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, h->D.fnno, cnt, h->D.u, d_tx,
+                                                      d_txb, d_txe, d_flux);
+  PM_CUDA(cudaGetLastError());
+  if (stream) PM_CUDA(cudaStreamSynchronize(s));
+  return check_elem_err(h);
+}
+
+int pm_stress(pm_handle hh, double* tx, double* txb, double* txe, double* flux) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !tx || !txb || !txe || !flux) return PM_E_ARG;
+  const size_t nn = (size_t)h->nnode;
+  double* d = nullptr;
+  PM_CUDA(cudaMalloc(&d, sizeof(double) * 21 * nn));
+  int st = pm_stress_dev(hh, d, d + 6 * nn, d + 12 * nn, d + 18 * nn, nullptr);
+  if (st == PM_OK) {
+    cudaMemcpy(tx, d, sizeof(double) * 6 * nn, cudaMemcpyDeviceToHost);
+    cudaMemcpy(txb, d + 6 * nn, sizeof(double) * 6 * nn, cudaMemcpyDeviceToHost);
+    cudaMemcpy(txe, d + 12 * nn, sizeof(double) * 6 * nn, cudaMemcpyDeviceToHost);
+    if (cudaMemcpy(flux, d + 18 * nn, sizeof(double) * 3 * nn, cudaMemcpyDeviceToHost) !=
+        cudaSuccess) {
+      h->err = "cudaMemcpy failed";
+      st = PM_E_CUDA;
+    }
+  }
+  cudaFree(d);
+  return st;
 }
 
 int pm_set_materials(pm_handle hh, const double* e, int numat) {

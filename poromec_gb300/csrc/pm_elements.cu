@@ -186,8 +186,10 @@ struct Geo {
 // Integration point geometry (thread-per-point).  Returns false when the
 // determinant is <= 1e-14, the condition jacob3d_m stops on.
 template <bool HEXA, typename T>
+__device__ bool point_geometry_rst(Geo<HEXA, T>& G, int gq, T r, T s, T t, T wq, T* huv);
+
+template <bool HEXA, typename T>
 __device__ bool point_geometry(Geo<HEXA, T>& G, int gq, T* huv) {
-  constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV;
   T r, s, t, wq;
   if (HEXA) {
     const int lz = gq >> 4, ly = (gq >> 2) & 3, lx = gq & 3;
@@ -197,6 +199,14 @@ __device__ bool point_geometry(Geo<HEXA, T>& G, int gq, T* huv) {
     r = T(cPRI4[gq]); s = T(cPSI4[gq]); t = T(cPTI4[gq]);
     wq = T(0.25);
   }
+  return point_geometry_rst<HEXA, T>(G, gq, r, s, t, wq, huv);
+}
+
+// The geometry of point (r, s, t) with quadrature weight wq into slot gq of G
+// (slots are the integration points, or the vertices for isw 3).
+template <bool HEXA, typename T>
+__device__ bool point_geometry_rst(Geo<HEXA, T>& G, int gq, T r, T s, T t, T wq, T* huv) {
+  constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV;
   T h[NV], hr[NV], hs[NV], ht[NV];
   if (HEXA) sf_hexa8<T>(r, s, t, h, hr, hs, ht);
   else sf_tetra4<T>(r, s, t, h, hr, hs, ht);
@@ -1027,6 +1037,105 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
   }
 }
 
+// ---------------------------------------------------------------------------
+// isw = 3: stresses and Darcy fluxes at the vertices (Elmlib03.f:2206-2256
+// hexa20, :440-495 tetra10), accumulated per vertex node for tform_pm's
+// average (Pform.f:433-640).  At vertex i (natural coordinates of the
+// element's vertex table): total stress D eps(u) - alpha dp_i, Biot stress
+// total + alpha p_i (normal components), flux perm (rho_f g - grad p) with
+// the linear pressure gradient.  One thread per vertex; one colour per
+// launch, so no two elements of a launch share a vertex.
+// ---------------------------------------------------------------------------
+__constant__ double cRNH[8] = {1, -1, -1, 1, 1, -1, -1, 1};
+__constant__ double cSNH[8] = {1, 1, -1, -1, 1, 1, -1, -1};
+__constant__ double cTNH[8] = {1, 1, 1, 1, -1, -1, -1, -1};
+__constant__ double cRNT[4] = {1, 0, 0, 0};
+__constant__ double cSNT[4] = {0, 1, 0, 0};
+__constant__ double cTNT[4] = {0, 0, 1, 0};
+
+template <bool HEXA>
+struct Sm3 {
+  Geo<HEXA, double> G;
+  double ul[3 * ET<HEXA>::NEN + ET<HEXA>::NV];
+  double dpl[ET<HEXA>::NV];
+  ElemCtx E;
+  int sFail;
+};
+
+template <bool HEXA>
+__global__ void __launch_bounds__(ET<HEXA>::NT)
+    k_stress3(ElemLaunch L, const double* __restrict__ u, const double* __restrict__ dp,
+              double* __restrict__ tx, double* __restrict__ txb, double* __restrict__ flux,
+              int* __restrict__ cnt) {
+  constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV, NT = ET<HEXA>::NT,
+                NST = 3 * NEN + NV;
+  extern __shared__ __align__(16) unsigned char smem[];
+  Sm3<HEXA>& S = *reinterpret_cast<Sm3<HEXA>*>(smem);
+  Geo<HEXA, double>& G = S.G;
+  ElemCtx& E = S.E;
+  const int el = L.elems[blockIdx.x];
+  if (threadIdx.x == 0) S.sFail = 0;
+  load_element<HEXA, double>(L, el, E, G);
+  for (int k = threadIdx.x; k < NST; k += NT) {
+    const int n = k < 3 * NEN ? E.nodes[k / 3] : E.nodes[k - 3 * NEN];
+    const int q = k < 3 * NEN ? k % 3 : 3;
+    S.ul[k] = u[(size_t)kNdf * (n - 1) + q];
+  }
+  for (int k = threadIdx.x; k < NV; k += NT) S.dpl[k] = dp[E.nodes[k] - 1];
+  __syncthreads();
+  const int i = threadIdx.x;
+  if (i < NV) {
+    const double r = HEXA ? cRNH[i] : cRNT[i], sv = HEXA ? cSNH[i] : cSNT[i],
+                 tv = HEXA ? cTNH[i] : cTNT[i];
+    if (!point_geometry_rst<HEXA, double>(G, i, r, sv, tv, 1.0, nullptr)) S.sFail = 1;
+  }
+  __syncthreads();
+  if (S.sFail) {
+    if (threadIdx.x == 0) atomicOr(L.err, 1);
+    return;
+  }
+  if (i >= NV) return;
+  const MatConst mc = L.mat[E.mat - 1];
+  double ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
+#pragma unroll
+  for (int k = 0; k < NEN; ++k) {
+    const double gx = G.g[i][k][0], gy = G.g[i][k][1], gz = G.g[i][k][2];
+    const double a0 = S.ul[3 * k], a1 = S.ul[3 * k + 1], a2 = S.ul[3 * k + 2];
+    ux += gx * a0; uy += gy * a0; uz += gz * a0;
+    vx += gx * a1; vy += gy * a1; vz += gz * a1;
+    wx += gx * a2; wy += gy * a2; wz += gz * a2;
+  }
+  const double e0 = ux, e1 = vy, e2 = wz, e3 = uy + vx, e4 = vz + wy, e5 = uz + wx;
+  const double A = mc.a, B = mc.b, C = mc.c;
+  const double dpm = mc.coef_biot * S.dpl[i];
+  const double pm = mc.coef_biot * S.ul[3 * NEN + i];
+  double t[6];
+  t[0] = (e0 + B * e1 + B * e2) * A - dpm;
+  t[1] = (B * e0 + e1 + B * e2) * A - dpm;
+  t[2] = (B * e0 + B * e1 + e2) * A - dpm;
+  t[3] = e3 * C * A;
+  t[4] = e4 * C * A;
+  t[5] = e5 * C * A;
+  double px = 0, py = 0, pz = 0;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const double pk = S.ul[3 * NEN + k];
+    px += G.gp[i][k][0] * pk; py += G.gp[i][k][1] * pk; pz += G.gp[i][k][2] * pk;
+  }
+  const int no = E.nodes[i] - 1;
+  double* T6 = tx + (size_t)6 * no;
+  double* B6 = txb + (size_t)6 * no;
+  for (int j = 0; j < 6; ++j) {
+    T6[j] += t[j];
+    B6[j] += t[j] + (j < 3 ? pm : 0.0);
+  }
+  double* F3 = flux + (size_t)3 * no;
+  F3[0] += mc.perm * (mc.fluid_d * L.g0 - px);
+  F3[1] += mc.perm * (mc.fluid_d * L.g1 - py);
+  F3[2] += mc.perm * (mc.fluid_d * L.g2 - pz);
+  cnt[no] += 1;
+}
+
 // isw = 5: initial stress, b -= int(B^T sigma0) with sigma0 interpolated by
 // the linear functions from the vertex values (Elmlib03.f:2528-2590).
 template <bool HEXA>
@@ -1161,6 +1270,17 @@ cudaError_t launch_adjoint(const ElemLaunch& L, bool hexa, int mode, const doubl
                      : launch_adjoint_t<true, 1>(L, lam, un, dun, mu, nu, grad, s);
   return mode == 0 ? launch_adjoint_t<false, 0>(L, lam, un, dun, mu, nu, grad, s)
                    : launch_adjoint_t<false, 1>(L, lam, un, dun, mu, nu, grad, s);
+}
+
+cudaError_t launch_stress3(const ElemLaunch& L, bool hexa, const double* u,
+                           const double* dp, double* tx, double* txb, double* flux, int* cnt,
+                           cudaStream_t s) {
+  if (L.nelem <= 0) return cudaSuccess;
+  if (hexa)
+    return launch_elem<Sm3<true>>(k_stress3<true>, L.nelem, 64, s, L, u, dp, tx, txb, flux,
+                                  cnt);
+  return launch_elem<Sm3<false>>(k_stress3<false>, L.nelem, 32, s, L, u, dp, tx, txb, flux,
+                                 cnt);
 }
 
 cudaError_t launch_stress5(const ElemLaunch& L, bool hexa, const double* tx0,

@@ -98,6 +98,9 @@ cudaError_t launch_rhs4(const ElemLaunch& L, bool hexa, const double* u,
 cudaError_t launch_adjoint(const ElemLaunch& L, bool hexa, int mode, const double* lam,
                            const double* un, const double* dun, double* mu, double* nu,
                            double* grad, cudaStream_t s);
+cudaError_t launch_stress3(const ElemLaunch& L, bool hexa, const double* u,
+                           const double* dp, double* tx, double* txb, double* flux, int* cnt,
+                           cudaStream_t s);
 cudaError_t launch_stress5(const ElemLaunch& L, bool hexa, const double* tx0,
                            double* b, cudaStream_t s);
 // Nodal kernels of the step driver (pm_capi.cu).

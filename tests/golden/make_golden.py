@@ -246,6 +246,18 @@ def convert(ref_root, kind, deck, prefix):
         p = os.path.join(ddir, "%s_up_node_%d.txt" % (prefix, n))
         if os.path.exists(p):
             hist[n] = read_history(p)
+    # tform_pm outputs of the same nodes: total, effective (stressE) and Biot
+    # (stressB) stress, Darcy flux
+    extra = {}
+    for key, tag in (("hist_stress", "stress"), ("hist_stressE", "stressE"),
+                     ("hist_stressB", "stressB"), ("hist_flux", "flux")):
+        rows = {}
+        for n in d["print_nodes"]:
+            pth = os.path.join(ddir, "%s_%s_node_%d.txt" % (prefix, tag, n))
+            if os.path.exists(pth):
+                rows[n] = read_history(pth)
+        if rows and sorted(rows) == sorted(hist):
+            extra[key] = np.stack([rows[n] for n in sorted(rows)])
     counts = read_counts(os.path.join(ddir, prefix + "_t_1.txt"))
     its = read_log(os.path.join(ddir, prefix + "_log_1.txt"))
     tol = d["solver_tol"] if d["solver_tol"] != 0.0 else 2.0 ** -53  # smachn
@@ -257,7 +269,7 @@ def convert(ref_root, kind, deck, prefix):
                maxit=d["maxit"], reord=int(d["reord"]), hist_nodes=hnodes,
                hist=np.stack([hist[n] for n in hnodes]) if len(hnodes) else np.zeros(0),
                pcg_iters=its, neq_ref=counts.get("neq", -1), nad_ref=counts.get("nad", -1),
-               nnode_ref=counts.get("nnode", -1), complete=int(not MISSING))
+               nnode_ref=counts.get("nnode", -1), complete=int(not MISSING), **extra)
     name = os.path.join(HERE, prefix + ".npz")
     np.savez_compressed(name, **out)
     return name, counts, nnode
