@@ -209,6 +209,13 @@ int pm_tune_spmv(pm_handle h, int* shape);
  * (total + p), and (3, nnode) the Darcy flux; vertex nodes average the values
  * of the elements that share them, mid-side nodes are zero.  The '_dev' form
  * takes device arrays (stream as pm_spmv_dev). */
+/* Nodal porosity (nnode; vertex nodes carry it): initial_porosity
+ * (Pform.f:1343-1432, material column 8 averaged over the elements sharing a
+ * vertex) at creation; every pm_step adds porosity_form's change
+ * (Pform.f:969-1175, Elmlib03.f:2605-2631 isw 7): the average over the
+ * elements at the vertex of alpha tr(eps(du)) + dp/M of the step's increments. */
+int pm_get_porosity(pm_handle h, double* poro);
+int pm_set_porosity(pm_handle h, const double* poro);
 int pm_stress(pm_handle h, double* tx, double* txb, double* txe, double* flux);
 int pm_stress_dev(pm_handle h, double* d_tx, double* d_txb, double* d_txe, double* d_flux,
                   void* stream);

@@ -143,6 +143,15 @@ class Oracle:
         _check(lib().or_stress(self.h, _p(tx), _p(txb), _p(txe), _p(fl)), "or_stress")
         return tx, txb, txe, fl
 
+    def get_porosity(self):
+        poro = np.zeros(self.nnode)
+        _check(lib().or_get_porosity(self.h, _p(poro)), "or_get_porosity")
+        return poro
+
+    def set_porosity(self, poro):
+        a = _f64(poro)
+        _check(lib().or_set_porosity(self.h, _p(a)), "or_set_porosity")
+
     def get_id(self):
         idr = np.zeros((self.nnode, 4), np.int32)
         _check(lib().or_get_id(self.h, _p(idr)), "or_get_id")

@@ -957,6 +957,33 @@ void element(bool hexa, const double* e, const int* iqm, const int* iqh,
       q[1] = m.perm * q[1];
       q[2] = m.perm * q[2];
     }
+  } else if (isw == 7) {
+    // porosity change at the vertices (Elmlib03.f:2605-2631 hexa20, the
+    // tetra10 twin in elmt15_pm): p(i) = alpha tr(eps(du)) + dp_i / M with u
+    // the step's increments
+    static const double RNH[8] = {1, -1, -1, 1, 1, -1, -1, 1};
+    static const double SNH[8] = {1, 1, -1, -1, 1, 1, -1, -1};
+    static const double TNH[8] = {1, 1, 1, 1, -1, -1, -1, -1};
+    static const double RNT[4] = {1, 0, 0, 0}, SNT[4] = {0, 1, 0, 0}, TNT[4] = {0, 0, 1, 0};
+    for (int i = 0; i < np; ++i) {
+      const double ri = hexa ? RNH[i] : RNT[i], si = hexa ? SNH[i] : SNT[i],
+                   ti = hexa ? TNH[i] : TNT[i];
+      if (hexa) {
+        sfhexa8_m(hp, hpx, hpy, hpz, ri, si, ti, false, true);
+        jacob3d_m(hpx, hpy, hpz, xj, xji, x, det, 8, true);
+        sfhexa20_m(hu, hux, huy, huz, ri, si, ti, false, true);
+        jacob3d_m(hux, huy, huz, xj, xji, x, det, 20, false);
+      } else {
+        sftetra4(hp, hpx, hpy, hpz, ri, si, ti, false, true);
+        jacob3d_m(hpx, hpy, hpz, xj, xji, x, det, 4, true);
+        sftetra10(hu, hux, huy, huz, ri, si, ti, false, true);
+        jacob3d_m(hux, huy, huz, xj, xji, x, det, 10, false);
+      }
+      double epsi[6];
+      deform3d(hux, huy, huz, u, epsi, nu);
+      const double pi = m.imod_biot * u[3 * nu + i];
+      p[i] = m.coef_biot * (epsi[0] + epsi[1] + epsi[2]) + pi;
+    }
   } else if (isw == 5) {
     for (int g = 0; g < ngp; ++g) {
       double ri, si, ti, wq, w;
@@ -1010,6 +1037,7 @@ struct or_handle_s {
   Loads L;
   Env env;
   std::vector<double> u, u0, dp, b0, b, x0, m, bst0;
+  std::vector<double> poro;  // nodal porosity (vertex nodes)
   bool fstress0 = false;
   int numcolors = 0;
   std::vector<int32_t> color_ptr, color_elems;  // elements grouped by colour
@@ -1428,6 +1456,8 @@ int pminres(or_handle_s* h, const double* m, const double* b, double* x,
 // ---------------------------------------------------------------------------
 extern "C" {
 
+static void initial_porosity(or_handle_s* h);
+
 int or_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndf,
               const int32_t* ix, const int32_t* id, const int32_t* fnno,
               const double* x, int numat, const int32_t* ie, const double* e,
@@ -1529,6 +1559,7 @@ int or_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndf,
                                  h->env.gravity[1] * h->env.gravity[1] +
                                  h->env.gravity[2] * h->env.gravity[2]);
   colour_mesh(h);
+  initial_porosity(h);
   *out = h;
   return OR_OK;
 }
@@ -1643,6 +1674,67 @@ int or_element(or_handle h, int nel, int isw, const double* ul,
 // order and averaged over the elements sharing the vertex; mid-side nodes
 // keep zeros.  tx, txb, txe (6, nnode), flux (3, nnode), from the current u
 // and dp.
+// initial_porosity (Pform.f:1343-1432): e(8) of the elements sharing a
+// vertex, averaged
+static void initial_porosity(or_handle_s* h) {
+  const int nnode = h->nnode, nenv = h->nenv, nen = h->nen;
+  std::vector<int> ic(nnode, 0);
+  h->poro.assign(nnode, 0.0);
+  for (int nel = 1; nel <= h->numel; ++nel) {
+    const int ma = h->ix[(size_t)(nen + 1) * (nel - 1) + nen];
+    const double poro = h->e[(size_t)OR_PROP * (ma - 1) + 7];
+    for (int i = 0; i < nenv; ++i) {
+      const int no = h->ix[(size_t)(nen + 1) * (nel - 1) + i];
+      if (no <= 0) continue;
+      ic[no - 1] += 1;
+      h->poro[no - 1] = h->poro[no - 1] + poro;
+    }
+  }
+  for (int i = 0; i < nnode; ++i)
+    if (h->fnno[i] == 1) h->poro[i] = h->poro[i] / ic[i];
+}
+
+// porosity_form (Pform.f:969-1175) with u = h->u
+static int porosity_form(or_handle_s* h) {
+  const int nnode = h->nnode, nenv = h->nenv, nen = h->nen;
+  std::vector<int> ic(nnode, 0);
+  std::vector<double> dporo(nnode, 0.0);
+  int ld[68], iqm[7], iqh[7];
+  double ul[68], xl[24], dpl[8], txn[48], pl[120], sdum[1];
+  for (int nel = 1; nel <= h->numel; ++nel) {
+    gather_element(h, nel, h->u.data(), ld, ul, xl, dpl, iqm, iqh, txn, nullptr);
+    const int ma = h->ix[(size_t)(nen + 1) * (nel - 1) + nen];
+    for (int i = 0; i < nenv; ++i) pl[i] = 0.0;
+    try {
+      element(h->hexa, &h->e[(size_t)OR_PROP * (ma - 1)], iqm, iqh, xl, ul, dpl, pl, sdum,
+              txn, 7, h->L, h->env);
+    } catch (DetError&) {
+      return OR_E_DET;
+    }
+    for (int i = 0; i < nenv; ++i) {
+      const int no = h->ix[(size_t)(nen + 1) * (nel - 1) + i];
+      if (no <= 0) continue;
+      ic[no - 1] += 1;
+      dporo[no - 1] = dporo[no - 1] + pl[i];
+    }
+  }
+  for (int i = 0; i < nnode; ++i)
+    if (h->fnno[i] == 1) h->poro[i] = h->poro[i] + dporo[i] / ic[i];
+  return OR_OK;
+}
+
+int or_get_porosity(or_handle h, double* poro) {
+  if (!h || !poro) return OR_E_ARG;
+  std::copy(h->poro.begin(), h->poro.end(), poro);
+  return OR_OK;
+}
+
+int or_set_porosity(or_handle h, const double* poro) {
+  if (!h || !poro) return OR_E_ARG;
+  h->poro.assign(poro, poro + h->nnode);
+  return OR_OK;
+}
+
 int or_stress(or_handle h, double* tx, double* txb, double* txe, double* flux) {
   if (!h || !tx || !txb || !txe || !flux) return OR_E_ARG;
   const int nnode = h->nnode, nenv = h->nenv, nen = h->nen;
@@ -1917,6 +2009,10 @@ int or_step(or_handle h, int maxnlit, double tol, int stop_crit, int solver,
     lhs = false;
   }
   loc.nlit = it;
+  // porosity_form (Pform.f:969-1175, elastic: no variable properties), on the
+  // increments before they are added to the state (Main.f:1086)
+  st = porosity_form(h);
+  if (st != OR_OK) return st;
   // update_res_v2 (Pload.f:483-540)
   for (int i = 1; i <= nnode; ++i) {
     for (int j = 1; j <= ndf - 1; ++j) {

@@ -95,6 +95,10 @@ int or_matvec(or_handle h, const double* x, double* y, int nthreads);
  * effective stress (6 per node) and Darcy flux (3 per node) at the vertices
  * from the current u and dp; mid-side nodes zero. */
 int or_stress(or_handle h, double* tx, double* txb, double* txe, double* flux);
+/* nodal porosity: initial_porosity (Pform.f:1343-1432) at creation, updated by
+ * porosity_form (Pform.f:969-1175) at the end of every or_step */
+int or_get_porosity(or_handle h, double* poro);
+int or_set_porosity(or_handle h, const double* poro);
 
 /* solv_pm (Solv.f:27-780): solver 1 = pcg (Iters.f:299-595), 7 = pminres
  * (Iters.f:3987-4305, 10 restarts), 11 = rpsqmr (Iters.f:6100-6439; no

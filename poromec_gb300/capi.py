@@ -87,6 +87,8 @@ def load(path=None):
     lib.pm_get_timers.argtypes = [c_p, c_p, c_i]
     lib.pm_set_materials.argtypes = [c_p, c_p, c_i]
     lib.pm_stress.argtypes = [c_p] * 5
+    lib.pm_get_porosity.argtypes = [c_p, c_p]
+    lib.pm_set_porosity.argtypes = [c_p, c_p]
     lib.pm_stress_dev.argtypes = [c_p] * 6
     lib.pm_adjoint_apply_dev.argtypes = [c_p] * 5
     lib.pm_adjoint_grad_dev.argtypes = [c_p] * 6
@@ -198,6 +200,15 @@ class Mesh:
 
     def set_refine(self, inner_tol=1e-5):
         self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
+
+    def get_porosity(self):
+        poro = np.zeros(self.nnode)
+        self._check(self.lib.pm_get_porosity(self.h, _p(poro)), "pm_get_porosity")
+        return poro
+
+    def set_porosity(self, poro):
+        a = np.ascontiguousarray(poro, dtype=np.float64)
+        self._check(self.lib.pm_set_porosity(self.h, _p(a)), "pm_set_porosity")
 
     def stress(self):
         """tform_pm isw 3 + effective_stress of the current state: total, Biot

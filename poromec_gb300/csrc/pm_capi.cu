@@ -125,7 +125,7 @@ __global__ void k_delta_update(int nnode, const int32_t* __restrict__ eq,
 // nodes keep zeros) and effective_stress (Pform.f:2487-2505): txe = tx + p
 // on the normal components
 __global__ void k_stress_finish(int nnode, const int32_t* __restrict__ fnno,
-                                const int* __restrict__ cnt, const double* __restrict__ u,
+                                const int32_t* __restrict__ cnt, const double* __restrict__ u,
                                 double* __restrict__ tx, double* __restrict__ txb,
                                 double* __restrict__ txe, double* __restrict__ flux) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
@@ -140,6 +140,14 @@ __global__ void k_stress_finish(int nnode, const int32_t* __restrict__ fnno,
     const double p = u[4 * (size_t)i + 3];
     for (int j = 0; j < 6; ++j) txe[6 * (size_t)i + j] = tx[6 * (size_t)i + j] + (j < 3 ? p : 0.0);
   }
+}
+
+// porosity_form's average (Pform.f:1150-1170, elastic: the change is added)
+__global__ void k_poro_finish(int nnode, const int32_t* __restrict__ fnno,
+                              const int32_t* __restrict__ cnt, const double* __restrict__ dporo,
+                              double* __restrict__ poro) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x)
+    if (fnno[i] == 1 && cnt[i] > 0) poro[i] = poro[i] + dporo[i] / (double)cnt[i];
 }
 
 // equation-space vector -> nodal layout (4 per node), zero on restrained dofs
@@ -947,6 +955,9 @@ int alloc_state(Handle* h) {
   PM_TRY(A(&D.u0, nn));
   PM_TRY(A(&D.f, nn));
   PM_TRY(A(&D.dp, h->nnode));
+  PM_TRY(A(&D.poro, h->nnode));
+  PM_TRY(A(&D.dporo, h->nnode));
+  PM_CUDA(cudaMalloc(&D.vcnt, sizeof(int32_t) * std::max(h->nnode, 1)));
   PM_TRY(A(&D.b0, n));
   PM_TRY(A(&D.b, n));
   PM_TRY(A(&D.bst0, n));
@@ -987,7 +998,7 @@ void free_all(Handle* h) {
   pm::Dev& D = h->D;
   pm::Panels& P = h->P;
   void* ptrs[] = {D.ix, D.eq, D.x, D.mat, D.slot, D.color_elems, D.eload, D.eloadp, D.nload,
-                  D.load, D.fload, D.dofkind, D.fnno, D.u, D.u0, D.dp, D.f, D.b0, D.b, D.bst0,
+                  D.load, D.fload, D.dofkind, D.fnno, D.u, D.u0, D.dp, D.poro, D.dporo, D.vcnt, D.f, D.b0, D.b, D.bst0,
                   D.ad, D.m, D.bx, D.by, D.rr, D.dx, D.xs, D.kv.x, D.kv.r, D.kv.z, D.kv.p, D.kv.q,
                   D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
@@ -1059,6 +1070,19 @@ int set_dev_array(Handle* h, T** dst, const T* src, size_t n) {
 // reference norms, its own decision); instances that have met their test
 // take no further solve (their correction is zero), the others solve
 // together in one batched PCG.
+// porosity_form (Pform.f:969-1175) on the step's increments held in D.u
+// (Main.f:1086 runs it after the nonlinear loop, before update_res_v2)
+int porosity_pass(Handle* h, cudaStream_t s) {
+  pm::Dev& D = h->D;
+  PM_CUDA(cudaMemsetAsync(D.dporo, 0, sizeof(double) * h->nnode, s));
+  for (int c = 0; c < h->numcolors; ++c)
+    PM_CUDA(pm::launch_poro7(elem_launch(h, c), h->hexa, D.u, D.dporo, s));
+  k_poro_finish<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.vcnt, D.dporo, D.poro);
+  PM_CUDA(cudaGetLastError());
+  h->launches += h->numcolors + 1;
+  return PM_OK;
+}
+
 int step_batch(Handle* h, int maxnlit, double tol, int stop_crit, int solver, int precond,
                double solvtol, int maxit, int reassemble, pm_step_info* info) {
   if (solver != 1 || h->precision == PM_FP32_REFINE) {
@@ -1182,6 +1206,7 @@ int step_batch(Handle* h, int maxnlit, double tol, int stop_crit, int solver, in
   }
   h->b_iters = iters;
   loc.nlit = it;
+  PM_TRY(porosity_pass(h, s));
   h->launches += 1;
   k_update_res<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0, D.dp);
   PM_CUDA(cudaGetLastError());
@@ -1281,6 +1306,28 @@ static int mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int 
   if ((st = pm::build_structure(h, ix, id, fnno, x, num)) != PM_OK) return fail(st);
   if ((st = alloc_state(h)) != PM_OK) return fail(st);
   if ((st = upload_materials(h)) != PM_OK) return fail(st);
+  {
+    // initial_porosity (Pform.f:1343-1432): e(8) averaged over the elements
+    // sharing a vertex; the counts are tform_pm's and porosity_form's ic
+    std::vector<int32_t> ic(nnode, 0);
+    std::vector<double> poro(nnode, 0.0);
+    for (int el = 0; el < numel; ++el) {
+      const int32_t* nd = ix + (size_t)(nen + 1) * el;
+      const double p0 = e[(size_t)PM_PROP * (nd[nen] - 1) + 7];
+      for (int a = 0; a < nenv; ++a)
+        if (nd[a] > 0) {
+          ic[nd[a] - 1] += 1;
+          poro[nd[a] - 1] += p0;
+        }
+    }
+    for (int i = 0; i < nnode; ++i)
+      if (fnno[i] == 1 && ic[i] > 0) poro[i] = poro[i] / ic[i];
+    if (cudaMemcpy(h->D.vcnt, ic.data(), sizeof(int32_t) * nnode, cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(h->D.poro, poro.data(), sizeof(double) * nnode, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+      return fail(PM_E_CUDA);
+  }
   if (ninst > 0 && (st = batch_setup(h)) != PM_OK) return fail(st);
   h->debug = getenv("PM_DEBUG") != nullptr;
   *out = reinterpret_cast<pm_handle>(h);
@@ -1663,6 +1710,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   }
   loc.nlit = it;
   PM_CUDA(cudaEventRecord(ev[5], s));
+  PM_TRY(porosity_pass(h, s));
   k_update_res<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0, D.dp);
   PM_CUDA(cudaGetLastError());
   PM_CUDA(cudaStreamSynchronize(s));
@@ -1678,6 +1726,22 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   return PM_OK;
 }
 
+int pm_get_porosity(pm_handle hh, double* poro) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !poro) return PM_E_ARG;
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  PM_CUDA(cudaMemcpy(poro, h->D.poro, sizeof(double) * h->nnode, cudaMemcpyDeviceToHost));
+  return PM_OK;
+}
+
+int pm_set_porosity(pm_handle hh, const double* poro) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || !poro) return PM_E_ARG;
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  PM_CUDA(cudaMemcpy(h->D.poro, poro, sizeof(double) * h->nnode, cudaMemcpyHostToDevice));
+  return PM_OK;
+}
+
 int pm_stress_dev(pm_handle hh, double* d_tx, double* d_txb, double* d_txe, double* d_flux,
                   void* stream) {
   Handle* h = reinterpret_cast<Handle*>(hh);
@@ -1686,16 +1750,14 @@ int pm_stress_dev(pm_handle hh, double* d_tx, double* d_txb, double* d_txe, doub
   // the state and the scratch belong to the handle's stream
   if (stream) PM_CUDA(cudaStreamSynchronize(h->stream));
   const size_t nn = (size_t)h->nnode;
-  int* cnt = reinterpret_cast<int*>(h->D.bx);  // scratch: nnode doubles hold nnode ints
   PM_CUDA(cudaMemsetAsync(d_tx, 0, sizeof(double) * 6 * nn, s));
   PM_CUDA(cudaMemsetAsync(d_txb, 0, sizeof(double) * 6 * nn, s));
   PM_CUDA(cudaMemsetAsync(d_flux, 0, sizeof(double) * 3 * nn, s));
-  PM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * nn, s));
   h->launches += h->numcolors + 1;
   for (int c = 0; c < h->numcolors; ++c)
     PM_CUDA(pm::launch_stress3(elem_launch(h, c), h->hexa, h->D.u, h->D.dp, d_tx, d_txb, d_flux,
-                               cnt, s));
-  k_stress_finish<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, h->D.fnno, cnt, h->D.u, d_tx,
+                               s));
+  k_stress_finish<<<grid_for(h->nnode), 256, 0, s>>>(h->nnode, h->D.fnno, h->D.vcnt, h->D.u, d_tx,
                                                       d_txb, d_txe, d_flux);
   PM_CUDA(cudaGetLastError());
   if (stream) PM_CUDA(cudaStreamSynchronize(s));

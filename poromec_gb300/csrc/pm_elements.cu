@@ -1044,7 +1044,9 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
 // element's vertex table): total stress D eps(u) - alpha dp_i, Biot stress
 // total + alpha p_i (normal components), flux perm (rho_f g - grad p) with
 // the linear pressure gradient.  One thread per vertex; one colour per
-// launch, so no two elements of a launch share a vertex.
+// launch, so no two elements of a launch share a vertex.  MODE 7 is the
+// porosity change of porosity_form (Pform.f:969-1175; Elmlib03.f:2605-2631):
+// alpha tr(eps(du)) + dp_i / M at vertex i, with u the step's increments.
 // ---------------------------------------------------------------------------
 __constant__ double cRNH[8] = {1, -1, -1, 1, 1, -1, -1, 1};
 __constant__ double cSNH[8] = {1, 1, -1, -1, 1, 1, -1, -1};
@@ -1062,11 +1064,10 @@ struct Sm3 {
   int sFail;
 };
 
-template <bool HEXA>
+template <bool HEXA, int MODE>
 __global__ void __launch_bounds__(ET<HEXA>::NT)
-    k_stress3(ElemLaunch L, const double* __restrict__ u, const double* __restrict__ dp,
-              double* __restrict__ tx, double* __restrict__ txb, double* __restrict__ flux,
-              int* __restrict__ cnt) {
+    k_vertex(ElemLaunch L, const double* __restrict__ u, const double* __restrict__ dp,
+             double* __restrict__ tx, double* __restrict__ txb, double* __restrict__ flux) {
   constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV, NT = ET<HEXA>::NT,
                 NST = 3 * NEN + NV;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1081,7 +1082,8 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     const int q = k < 3 * NEN ? k % 3 : 3;
     S.ul[k] = u[(size_t)kNdf * (n - 1) + q];
   }
-  for (int k = threadIdx.x; k < NV; k += NT) S.dpl[k] = dp[E.nodes[k] - 1];
+  if (MODE == 3)
+    for (int k = threadIdx.x; k < NV; k += NT) S.dpl[k] = dp[E.nodes[k] - 1];
   __syncthreads();
   const int i = threadIdx.x;
   if (i < NV) {
@@ -1105,6 +1107,12 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     vx += gx * a1; vy += gy * a1; vz += gz * a1;
     wx += gx * a2; wy += gy * a2; wz += gz * a2;
   }
+  const int no = E.nodes[i] - 1;
+  if (MODE == 7) {
+    // tx is the porosity change accumulator here
+    tx[no] += mc.coef_biot * (ux + vy + wz) + mc.imod_biot * S.ul[3 * NEN + i];
+    return;
+  }
   const double e0 = ux, e1 = vy, e2 = wz, e3 = uy + vx, e4 = vz + wy, e5 = uz + wx;
   const double A = mc.a, B = mc.b, C = mc.c;
   const double dpm = mc.coef_biot * S.dpl[i];
@@ -1122,7 +1130,6 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     const double pk = S.ul[3 * NEN + k];
     px += G.gp[i][k][0] * pk; py += G.gp[i][k][1] * pk; pz += G.gp[i][k][2] * pk;
   }
-  const int no = E.nodes[i] - 1;
   double* T6 = tx + (size_t)6 * no;
   double* B6 = txb + (size_t)6 * no;
   for (int j = 0; j < 6; ++j) {
@@ -1133,7 +1140,6 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
   F3[0] += mc.perm * (mc.fluid_d * L.g0 - px);
   F3[1] += mc.perm * (mc.fluid_d * L.g1 - py);
   F3[2] += mc.perm * (mc.fluid_d * L.g2 - pz);
-  cnt[no] += 1;
 }
 
 // isw = 5: initial stress, b -= int(B^T sigma0) with sigma0 interpolated by
@@ -1273,14 +1279,24 @@ cudaError_t launch_adjoint(const ElemLaunch& L, bool hexa, int mode, const doubl
 }
 
 cudaError_t launch_stress3(const ElemLaunch& L, bool hexa, const double* u,
-                           const double* dp, double* tx, double* txb, double* flux, int* cnt,
+                           const double* dp, double* tx, double* txb, double* flux,
                            cudaStream_t s) {
   if (L.nelem <= 0) return cudaSuccess;
   if (hexa)
-    return launch_elem<Sm3<true>>(k_stress3<true>, L.nelem, 64, s, L, u, dp, tx, txb, flux,
-                                  cnt);
-  return launch_elem<Sm3<false>>(k_stress3<false>, L.nelem, 32, s, L, u, dp, tx, txb, flux,
-                                 cnt);
+    return launch_elem<Sm3<true>>(k_vertex<true, 3>, L.nelem, 64, s, L, u, dp, tx, txb, flux);
+  return launch_elem<Sm3<false>>(k_vertex<false, 3>, L.nelem, 32, s, L, u, dp, tx, txb, flux);
+}
+
+cudaError_t launch_poro7(const ElemLaunch& L, bool hexa, const double* du, double* dporo,
+                         cudaStream_t s) {
+  if (L.nelem <= 0) return cudaSuccess;
+  if (hexa)
+    return launch_elem<Sm3<true>>(k_vertex<true, 7>, L.nelem, 64, s, L, du,
+                                  (const double*)nullptr, dporo, (double*)nullptr,
+                                  (double*)nullptr);
+  return launch_elem<Sm3<false>>(k_vertex<false, 7>, L.nelem, 32, s, L, du,
+                                 (const double*)nullptr, dporo, (double*)nullptr,
+                                 (double*)nullptr);
 }
 
 cudaError_t launch_stress5(const ElemLaunch& L, bool hexa, const double* tx0,

@@ -99,8 +99,10 @@ cudaError_t launch_adjoint(const ElemLaunch& L, bool hexa, int mode, const doubl
                            const double* un, const double* dun, double* mu, double* nu,
                            double* grad, cudaStream_t s);
 cudaError_t launch_stress3(const ElemLaunch& L, bool hexa, const double* u,
-                           const double* dp, double* tx, double* txb, double* flux, int* cnt,
+                           const double* dp, double* tx, double* txb, double* flux,
                            cudaStream_t s);
+cudaError_t launch_poro7(const ElemLaunch& L, bool hexa, const double* du, double* dporo,
+                         cudaStream_t s);
 cudaError_t launch_stress5(const ElemLaunch& L, bool hexa, const double* tx0,
                            double* b, cudaStream_t s);
 // Nodal kernels of the step driver (pm_capi.cu).
@@ -121,6 +123,8 @@ struct Dev {
   int32_t* dofkind = nullptr;      // per equation: 0 displacement, 1 pressure
   int32_t* fnno = nullptr;
   double *u = nullptr, *u0 = nullptr, *dp = nullptr, *f = nullptr;
+  double *poro = nullptr, *dporo = nullptr;  // nodal porosity and its step change
+  int32_t* vcnt = nullptr;                    // elements sharing each vertex node
   double *b0 = nullptr, *b = nullptr, *bst0 = nullptr;
   double *ad = nullptr, *m = nullptr;
   double *bx = nullptr, *by = nullptr;   // staging vectors for host calls

@@ -97,3 +97,69 @@ def test_stress_dev_on_torch_stream():
     ref = m.stress()
     for a, b in zip((tx, txb, txe, fl), ref):
         assert np.array_equal(a.cpu().numpy(), b)
+
+
+def _poro_fixture(fx, poro0=0.3):
+    fx = dict(fx)
+    fx["e"] = np.array(fx["e"], float).copy()
+    fx["e"][:, 7] = poro0
+    E, nu, _, M, alpha = fx["e"][0][:5]
+    k_tr = E * (1 - nu) / ((1 + nu) * (1 - 2 * nu)) * (1 + 2 * nu / (1 - nu))
+    return fx, k_tr, M, alpha
+
+
+def test_porosity_golden_derived_on_gpu(golden):
+    """porosity_form on the GPU against the golden hexa20 run: the summed
+    changes equal alpha avg tr(eps(u_N)) + dp_N/M, with avg tr(eps) from the
+    printed total stress (normals sum to a (1 + 2b) tr(eps) - 3 alpha dp)."""
+    fx, k_tr, M, alpha = _poro_fixture(golden("exemplo1_mesh0_t2"))
+    m = pg.from_problem(fx)
+    worst = 0.0
+    for k in range(1, 601):
+        m.step(maxnlit=2, stop_crit=1, solvtol=float(fx["solver_tol"]), maxit=int(fx["maxit"]))
+        poro = m.get_porosity()
+        for a, n in enumerate(fx["hist_nodes"]):
+            dpn = fx["hist"][a][k][5] - fx["hist"][a][0][5]
+            sn = fx["hist_stress"][a][k][2:5].sum()
+            ref = 0.3 + alpha * (sn + 3 * alpha * dpn) / k_tr + dpn / M
+            worst = max(worst, abs(poro[n - 1] - ref))
+    assert worst < 1e-10, worst
+
+
+@pytest.mark.parametrize("name", ["exemplo1_mesh0_t2", "exemplo1_mesh0_t2_tetra"])
+def test_porosity_stress_relation_on_gpu(golden, name):
+    fx, k_tr, M, alpha = _poro_fixture(golden(name))
+    m = pg.from_problem(fx)
+    v = fx["fnno"] == 1
+    for _ in range(5):
+        m.step(maxnlit=2, stop_crit=1, solvtol=float(fx["solver_tol"]), maxit=int(fx["maxit"]))
+    poro = m.get_porosity()
+    tx, _, _, _ = m.stress()
+    _, _, dp = m.get_state()
+    ref = 0.3 + alpha * (tx[v, :3].sum(1) + 3 * alpha * dp[v]) / k_tr + dp[v] / M
+    assert np.abs(poro[v] - ref).max() < 1e-12
+    assert not np.any(poro[~v])
+
+
+@pytest.mark.parametrize("which", ["tetra", "cube"])
+def test_porosity_matches_oracle(which):
+    """Per-element materials (cube) and distorted tetra10: GPU and oracle
+    step independently; their states agree to the solver tolerance, so the
+    porosity changes are compared at 1e-9 of their largest magnitude."""
+    pb = {"tetra": lambda: meshgen.tetra_problem(n=3),
+          "cube": lambda: meshgen.cube_problem(n=4)}[which]()
+    e = np.array(pb["e"], float).reshape(-1, oracle.PROP).copy()
+    e[:, 7] = np.random.default_rng(11).uniform(0.1, 0.4, len(e))
+    pb = dict(pb)
+    pb["e"] = e
+    m = pg.from_problem(pb)
+    o = _oracle(pb)
+    p0 = o.get_porosity()
+    assert np.array_equal(m.get_porosity(), p0)
+    for _ in range(3):
+        m.step(maxnlit=2, stop_crit=1, solvtol=1e-13, maxit=200000)
+        o.step(maxnlit=2, stop_crit=1, solvtol=1e-13, maxit=200000)
+        dg, do = m.get_porosity() - p0, o.get_porosity() - p0
+        assert np.abs(dg - do).max() < 1e-9 * np.abs(do).max()
+    m.set_porosity(p0)
+    assert np.array_equal(m.get_porosity(), p0)
