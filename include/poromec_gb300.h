@@ -145,14 +145,22 @@ int pm_assemble(pm_handle h, int isw, int lhs, int rhs, const double* u, double*
 int pm_spmv(pm_handle h, const double* x, double* y);
 
 /* solv_pm (Solv.f:27-780): solver 1 = PCG (Iters.f:299-595),
+ * 2 = GMRES(l) (gmres2, Iters.f:1411-1700; FP64 only; maxit counts cycles of
+ * nkrylov iterations, see pm_set_nkrylov),
  * 7 = preconditioned MINRES (Iters.f:3987-4305, 10 restarts),
  * 11 = rpsqmr (Iters.f:6100-6439, the reference's default; FP64 only; where
- * it does not converge in maxit the reference switches to GMRES(l), here the
- * call returns PM_E_NOCONV); precond 2 = diag 1/ad, 5 = |1/ad|
+ * it does not converge in maxit it switches to GMRES(l) from x = 0 with maxit
+ * cycles, Solv.f:765, and info->iters counts both); precond 2 = diag 1/ad,
+ * 5 = |1/ad|
  * (Precond.f:22-79).  x is set to 0 first (fnew = .true.).  b, x host arrays
  * of length neq. */
 int pm_solve(pm_handle h, int solver, int precond, const double* b, double* x,
              double tol, int maxit, pm_step_info* info);
+
+/* GMRES(l) basis size (ngram, default 150, Main.f:274; solver-file key
+ * nkrylov, Rdata.f:3222-3229).  The (nkrylov + 1) x neq basis is allocated on
+ * the first GMRES solve. */
+int pm_set_nkrylov(pm_handle h, int nkrylov);
 
 /* One 'solv' macro step (Main.f:876-1123) on the device-resident state:
  * pload_pm, isw 4 loop, predictor, nonlinear loop (isw 2, residual check

@@ -143,6 +143,9 @@ class Oracle:
         _check(lib().or_stress(self.h, _p(tx), _p(txb), _p(txe), _p(fl)), "or_stress")
         return tx, txb, txe, fl
 
+    def set_nkrylov(self, k):
+        _check(lib().or_set_nkrylov(self.h, int(k)), "or_set_nkrylov")
+
     def get_porosity(self):
         poro = np.zeros(self.nnode)
         _check(lib().or_get_porosity(self.h, _p(poro)), "or_get_porosity")

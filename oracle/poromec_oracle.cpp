@@ -1038,6 +1038,7 @@ struct or_handle_s {
   Env env;
   std::vector<double> u, u0, dp, b0, b, x0, m, bst0;
   std::vector<double> poro;  // nodal porosity (vertex nodes)
+  int nkrylov = 150;         // GMRES(l) basis size, ngram (Main.f:274)
   bool fstress0 = false;
   int numcolors = 0;
   std::vector<int32_t> color_ptr, color_elems;  // elements grouped by colour
@@ -1723,6 +1724,12 @@ static int porosity_form(or_handle_s* h) {
   return OR_OK;
 }
 
+int or_set_nkrylov(or_handle h, int nkrylov) {
+  if (!h || nkrylov < 1) return OR_E_ARG;
+  h->nkrylov = nkrylov;
+  return OR_OK;
+}
+
 int or_get_porosity(or_handle h, double* poro) {
   if (!h || !poro) return OR_E_ARG;
   std::copy(h->poro.begin(), h->poro.end(), poro);
@@ -1805,7 +1812,7 @@ int or_pform_range(or_handle h, int isw, int lhs, int rhs, const double* u,
 // GMRES(l), Solv.f:707-766); sigma = 0 or rho = 0 are breakdowns
 // (stop_mef in the reference).
 int rpsqmr(or_handle_s* h, const double* m, const double* b, double* x, double tol,
-           int maxit, int nth, or_step_info* info) {
+           int maxit, int nth, or_step_info* info, bool* reached_maxit = nullptr) {
   const int neq = h->neq;
   for (int i = 0; i < neq; ++i)
     if (h->ad[i] == 0.0) return OR_E_ZERO_DIAG;
@@ -1856,7 +1863,132 @@ int rpsqmr(or_handle_s* h, const double* m, const double* b, double* x, double t
     info->iters = converged ? j : maxit;
     info->conv = conv;
   }
+  if (!converged) {
+    if (reached_maxit) *reached_maxit = true;
+    return OR_E_NOCONV;
+  }
+  matvec(h, x, t.data(), nth);
+  if (info) info->xkx = dot(x, t.data(), neq, nth);
+  return OR_OK;
+}
+
+// sym_ortho2 (Iters.f:6718-6745): the Givens rotation of GMRES
+static void sym_ortho2(double a, double b, double& c, double& s, double& r) {
+  const double ma = std::fabs(a), mb = std::fabs(b);
+  c = 1.0;
+  s = 0.0;
+  r = a;
+  if (b != 0.0) {
+    if (mb > ma) {
+      const double t = a / b;
+      s = 1.0 / std::sqrt(1.0 + t * t);
+      c = s * t;
+      r = b / s;
+    } else {
+      const double t = b / a;
+      c = 1.0 / std::sqrt(1.0 + t * t);
+      s = c * t;
+      r = a / c;
+    }
+  }
+}
+
+// gmres2 (Iters.f:1411-1700): restarted GMRES(k) with the diagonal
+// preconditioner on the left, modified Gram-Schmidt with one more pass when
+// the norm drops below kesp = 0.25 of its value before orthogonalisation,
+// Givens QR of the Hessenberg matrix.  maxit counts cycles.  x starts at 0
+// (fnew); conv = tol ||M b||; a run that ends its cycles above conv is the
+// reference's stop_mef (OR_E_NOCONV here).  A zero right-hand side returns
+// x = 0 (the reference divides by the zero residual norm there).
+int gmres2(or_handle_s* h, const double* m, const double* b, double* x, double tol,
+           int maxit, int k, int nth, or_step_info* info) {
+  const int neq = h->neq;
+  const double kesp = 0.25;
+  std::vector<double> g((size_t)neq * (k + 1)), hm((size_t)(k + 1) * k, 0.0);
+  std::vector<double> y(k), c(k), sv(k), e(k + 1);
+  auto G = [&](int j) { return g.data() + (size_t)neq * (j - 1); };  // g(1, j)
+  auto H = [&](int i, int j) -> double& { return hm[(size_t)(k + 1) * (j - 1) + (i - 1)]; };
+  for (int i = 0; i < neq; ++i) {
+    x[i] = 0.0;
+    G(1)[i] = b[i] * m[i];
+  }
+  double norm = std::sqrt(dot(G(1), G(1), neq, nth));
+  const double econv = tol * norm;
+  if (info) info->conv = econv;
+  if (norm == 0.0) {
+    if (info) info->iters = 0;
+    return OR_OK;
+  }
+  int nit = 0, ni = 0;
+  bool converged = false;
+  for (int l = 1; l <= maxit; ++l) {
+    matvec(h, x, G(1), nth);
+    for (int i = 0; i < neq; ++i) G(1)[i] = (b[i] - G(1)[i]) * m[i];
+    e[0] = std::sqrt(dot(G(1), G(1), neq, nth));
+    double inorm = 1.0 / e[0];
+    for (int i = 0; i < neq; ++i) G(1)[i] = G(1)[i] * inorm;
+    ni = 0;
+    for (int i = 1; i <= k; ++i) {
+      ++nit;
+      ++ni;
+      double* w = G(i + 1);
+      matvec(h, G(i), w, nth);
+      for (int j = 0; j < neq; ++j) w[j] = w[j] * m[j];
+      const double tau = std::sqrt(dot(w, w, neq, nth));
+      for (int j = 1; j <= i; ++j) {
+        const double beta = dot(w, G(j), neq, nth);
+        const double* gj = G(j);
+        for (int ic = 0; ic < neq; ++ic) w[ic] = w[ic] - beta * gj[ic];
+        H(j, i) = beta;
+      }
+      norm = std::sqrt(dot(w, w, neq, nth));
+      if (norm <= kesp * tau) {
+        for (int j = 1; j <= i; ++j) {
+          const double beta = dot(w, G(j), neq, nth);
+          const double* gj = G(j);
+          for (int ic = 0; ic < neq; ++ic) w[ic] = w[ic] - beta * gj[ic];
+          H(j, i) = H(j, i) + beta;
+        }
+      }
+      norm = std::sqrt(dot(w, w, neq, nth));
+      H(i + 1, i) = norm;
+      inorm = 1.0 / norm;
+      for (int ic = 0; ic < neq; ++ic) w[ic] = w[ic] * inorm;
+      for (int j = 1; j <= i - 1; ++j) {
+        const double aux1 = c[j - 1] * H(j, i) + sv[j - 1] * H(j + 1, i);
+        const double aux2 = -sv[j - 1] * H(j, i) + c[j - 1] * H(j + 1, i);
+        H(j, i) = aux1;
+        H(j + 1, i) = aux2;
+      }
+      double r;
+      sym_ortho2(H(i, i), H(i + 1, i), c[i - 1], sv[i - 1], r);
+      H(i, i) = r;
+      H(i + 1, i) = 0.0;
+      e[i] = -sv[i - 1] * e[i - 1];
+      e[i - 1] = c[i - 1] * e[i - 1];
+      if (std::fabs(e[i]) <= econv) break;
+    }
+    // back substitution R y = e
+    for (int j = 1; j <= ni; ++j) y[j - 1] = e[j - 1];
+    for (int j = ni; j >= 2; --j) {
+      y[j - 1] = y[j - 1] / H(j, j);
+      const double r = y[j - 1];
+      for (int i = 1; i <= j - 1; ++i) y[i - 1] = y[i - 1] - H(i, j) * r;
+    }
+    y[0] = y[0] / H(1, 1);
+    for (int j = 1; j <= ni; ++j) {
+      const double r = y[j - 1];
+      const double* gj = G(j);
+      for (int i = 0; i < neq; ++i) x[i] = x[i] + r * gj[i];
+    }
+    if (std::fabs(e[ni]) <= econv) {
+      converged = true;
+      break;
+    }
+  }
+  if (info) info->iters = nit;
   if (!converged) return OR_E_NOCONV;
+  std::vector<double> t(neq);
   matvec(h, x, t.data(), nth);
   if (info) info->xkx = dot(x, t.data(), neq, nth);
   return OR_OK;
@@ -1880,7 +2012,17 @@ int or_solve(or_handle h, int solver, int precond, const double* b, double* x,
   }
   if (solver == 1) return pcg(h, h->m.data(), b, x, tol, maxit, nthreads, info);
   if (solver == 7) return pminres(h, h->m.data(), b, x, tol, maxit, nthreads, info);
-  if (solver == 11) return rpsqmr(h, h->m.data(), b, x, tol, maxit, nthreads, info);
+  if (solver == 2) return gmres2(h, h->m.data(), b, x, tol, maxit, h->nkrylov, nthreads, info);
+  if (solver == 11) {
+    // Solv.f:707-766: rpsqmr, and GMRES(l) from x = 0 when it reaches maxit
+    bool fallback = false;
+    const int st = rpsqmr(h, h->m.data(), b, x, tol, maxit, nthreads, info, &fallback);
+    if (!fallback) return st;
+    const int its = info ? info->iters : 0;
+    const int st2 = gmres2(h, h->m.data(), b, x, tol, maxit, h->nkrylov, nthreads, info);
+    if (info) info->iters += its;
+    return st2;
+  }
   return OR_E_ARG;
 }
 

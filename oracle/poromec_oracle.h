@@ -97,13 +97,17 @@ int or_matvec(or_handle h, const double* x, double* y, int nthreads);
 int or_stress(or_handle h, double* tx, double* txb, double* txe, double* flux);
 /* nodal porosity: initial_porosity (Pform.f:1343-1432) at creation, updated by
  * porosity_form (Pform.f:969-1175) at the end of every or_step */
+/* GMRES(l) basis size (ngram, default 150, Main.f:274; solver file key
+ * nkrylov, Rdata.f:3222-3229) used by solver 2 and by the rpsqmr fallback */
+int or_set_nkrylov(or_handle h, int nkrylov);
 int or_get_porosity(or_handle h, double* poro);
 int or_set_porosity(or_handle h, const double* poro);
 
-/* solv_pm (Solv.f:27-780): solver 1 = pcg (Iters.f:299-595), 7 = pminres
- * (Iters.f:3987-4305, 10 restarts), 11 = rpsqmr (Iters.f:6100-6439; no
- * convergence returns OR_E_NOCONV where the reference switches to GMRES(l));
- * precond 2 = 1/ad, 5 = |1/ad|
+/* solv_pm (Solv.f:27-780): solver 1 = pcg (Iters.f:299-595), 2 = gmres2
+ * (Iters.f:1411-1700, maxit = cycles of nkrylov iterations), 7 = pminres
+ * (Iters.f:3987-4305, 10 restarts), 11 = rpsqmr (Iters.f:6100-6439), which
+ * switches to gmres2 from x = 0 when it reaches maxit (Solv.f:765; info->iters
+ * then counts both); precond 2 = 1/ad, 5 = |1/ad|
  * (Precond.f:22-79).  x is zeroed first (fnew = .true.). */
 int or_solve(or_handle h, int solver, int precond, const double* b, double* x,
              double tol, int maxit, int nthreads, or_step_info* info);

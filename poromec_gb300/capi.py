@@ -88,6 +88,7 @@ def load(path=None):
     lib.pm_set_materials.argtypes = [c_p, c_p, c_i]
     lib.pm_stress.argtypes = [c_p] * 5
     lib.pm_get_porosity.argtypes = [c_p, c_p]
+    lib.pm_set_nkrylov.argtypes = [c_p, c_i]
     lib.pm_set_porosity.argtypes = [c_p, c_p]
     lib.pm_stress_dev.argtypes = [c_p] * 6
     lib.pm_adjoint_apply_dev.argtypes = [c_p] * 5
@@ -201,6 +202,10 @@ class Mesh:
     def set_refine(self, inner_tol=1e-5):
         self._check(self.lib.pm_set_refine(self.h, float(inner_tol)), "pm_set_refine")
 
+    def set_nkrylov(self, k):
+        """GMRES(l) basis size (default 150)."""
+        self._check(self.lib.pm_set_nkrylov(self.h, int(k)), "pm_set_nkrylov")
+
     def get_porosity(self):
         poro = np.zeros(self.nnode)
         self._check(self.lib.pm_get_porosity(self.h, _p(poro)), "pm_get_porosity")
@@ -301,7 +306,8 @@ class Mesh:
         return y
 
     def solve(self, b, solver=1, precond=2, tol=1e-11, maxit=50000):
-        """solv_pm (Solv.f:27-780): solver 1 PCG, 7 MINRES."""
+        """solv_pm (Solv.f:27-780): solver 1 PCG, 2 GMRES(l) (maxit = cycles),
+        7 MINRES, 11 rpsqmr (GMRES(l) fallback at maxit)."""
         ba = _f64(b)
         x = np.zeros(self.neq)
         info = StepInfo()

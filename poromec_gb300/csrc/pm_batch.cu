@@ -12,28 +12,10 @@
 #include <cuda_runtime.h>
 
 #include "pm_krylov.h"
+#include "pm_reduce.h"
 
 namespace pm {
 namespace {
-
-__device__ __forceinline__ double bwarp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-__device__ double bblock_sum(double v, double* sh) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  v = bwarp_sum(v);
-  __syncthreads();
-  if (lane == 0) sh[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
-    v = bwarp_sum(v);
-  }
-  return v;
-}
 
 // The block's instance and equation range [e0, e1).
 __device__ __forceinline__ int seg_range(const BatchView& B, int& e0, int& e1) {
@@ -53,7 +35,7 @@ __device__ bool seg_reduce(const BatchView& B, int inst, const double (&v)[NV],
   __shared__ bool last;
   double bs[NV];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) bs[k] = bblock_sum(v[k], sh);
+  for (int k = 0; k < NV; ++k) bs[k] = block_sum(v[k], sh);
   const int b0 = B.blk_ptr[inst], b1 = B.blk_ptr[inst + 1];
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -70,7 +52,7 @@ __device__ bool seg_reduce(const BatchView& B, int inst, const double (&v)[NV],
     double s = 0.0;
     for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x)
       s += __ldcg(&B.partial[(size_t)k * B.nblk + i]);
-    tot[k] = bblock_sum(s, sh);
+    tot[k] = block_sum(s, sh);
   }
   if (threadIdx.x == 0) B.counter[inst] = 0u;
   return true;

@@ -324,6 +324,170 @@ int run_graph(Handle* h, cudaGraphExec_t g, pm::KrylovScalars* ks) {
   }
 }
 
+// sym_ortho2 (Iters.f:6718-6745)
+void sym_ortho2(double a, double b, double& c, double& s, double& r) {
+  const double ma = std::fabs(a), mb = std::fabs(b);
+  c = 1.0;
+  s = 0.0;
+  r = a;
+  if (b != 0.0) {
+    if (mb > ma) {
+      const double t = a / b;
+      s = 1.0 / std::sqrt(1.0 + t * t);
+      c = s * t;
+      r = b / s;
+    } else {
+      const double t = b / a;
+      c = 1.0 / std::sqrt(1.0 + t * t);
+      s = c * t;
+      r = a / c;
+    }
+  }
+}
+
+// gmres2 (Iters.f:1411-1700) on the device: restarted GMRES(k), diagonal
+// preconditioner on the left, modified Gram-Schmidt with a second pass when
+// |w| drops to kesp = 0.25 of its value before orthogonalisation, Givens QR.
+// maxit counts cycles; x (device) starts at 0; conv = tol |M b|.  The basis
+// and scalars live in HBM; the host keeps H, the rotations and e (k + 1
+// values) and reads the step's dot products once per Arnoldi step (twice
+// with the second pass).
+int gmres_run(Handle* h, const double* d_b, double* x, double tol, int maxit, int* nit_out,
+              double* econv_out) {
+  const int n = h->neq, k = h->nkrylov;
+  pm::Dev& D = h->D;
+  cudaStream_t st = h->stream;
+  if (h->gm_alloc_k < k) {
+    for (double** p : {&D.gm_basis, &D.gm_scal, &D.gm_y})
+      if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+      }
+    h->gm_alloc_k = 0;
+    if (cudaMalloc(&D.gm_basis, sizeof(double) * (size_t)(k + 1) * n) != cudaSuccess ||
+        cudaMalloc(&D.gm_scal, sizeof(double) * (size_t)(2 * k + 4)) != cudaSuccess ||
+        cudaMalloc(&D.gm_y, sizeof(double) * (size_t)k) != cudaSuccess) {
+      cudaGetLastError();
+      h->err = "GMRES(l): cannot allocate the Krylov basis ((nkrylov + 1) x neq doubles)";
+      return PM_E_NOMEM;
+    }
+    h->gm_alloc_k = k;
+  }
+  const pm::PanelView P = h->P.view();
+  const double* val64 = h->P.val;
+  double* G = D.gm_basis;
+  double* gs = D.gm_scal;
+  auto g = [&](int j) { return G + (size_t)(j - 1) * n; };
+  std::vector<double> H((size_t)(k + 1) * k, 0.0), c(k), sn(k), e(k + 1), y(k), hs(2 * k + 4);
+  auto Hm = [&](int i, int j) -> double& { return H[(size_t)(k + 1) * (j - 1) + (i - 1)]; };
+  auto read = [&](int a, int cnt) -> int {
+    PM_CUDA(cudaMemcpyAsync(hs.data() + a, gs + a, sizeof(double) * cnt,
+                            cudaMemcpyDeviceToHost, st));
+    PM_CUDA(cudaStreamSynchronize(st));
+    return PM_OK;
+  };
+  const double kesp = 0.25;
+  PM_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, st));
+  PM_CUDA(pm::gm_resid(n, d_b, nullptr, D.m, g(1), gs, D.partial, D.counter, st));
+  PM_TRY(read(0, 1));
+  h->launches += 1;
+  double norm = std::sqrt(hs[0]);
+  const double econv = tol * norm;
+  *econv_out = econv;
+  *nit_out = 0;
+  if (norm == 0.0) return PM_OK;
+  int nit = 0, ni = 0;
+  for (int l = 1; l <= maxit; ++l) {
+    PM_CUDA(pm::spmv(P, val64, x, g(1), 0, nullptr, nullptr, nullptr, st));
+    PM_CUDA(pm::gm_resid(n, d_b, g(1), D.m, g(1), gs, D.partial, D.counter, st));
+    PM_TRY(read(0, 1));
+    e[0] = std::sqrt(hs[0]);
+    if (!(e[0] > 0.0) || !std::isfinite(e[0])) {
+      if (e[0] == 0.0) break;  // x solves the system exactly
+      h->err = "GMRES(l): non-finite residual";
+      *nit_out = nit;
+      return PM_E_NOCONV;
+    }
+    PM_CUDA(pm::gm_scale(n, g(1), 1.0 / e[0], st));
+    h->launches += 3;
+    ni = 0;
+    for (int i = 1; i <= k; ++i) {
+      ++nit;
+      ++ni;
+      double* w = g(i + 1);
+      PM_CUDA(pm::spmv(P, val64, g(i), w, 0, nullptr, nullptr, nullptr, st));
+      PM_CUDA(pm::gm_first(n, w, D.m, g(1), gs, D.partial, D.counter, st));
+      for (int j = 1; j <= i; ++j)
+        PM_CUDA(pm::gm_mgs(n, w, g(j), j < i ? g(j + 1) : nullptr, gs + j,
+                           j < i ? gs + j + 1 : gs + k + 1, D.partial, D.counter, st));
+      h->launches += 2 + i;
+      PM_TRY(read(0, k + 2));
+      const double tau = std::sqrt(hs[0]);
+      for (int j = 1; j <= i; ++j) Hm(j, i) = hs[j];
+      norm = std::sqrt(hs[k + 1]);
+      if (norm <= kesp * tau) {
+        PM_CUDA(pm::gm_dot(n, w, g(1), gs + k + 3, D.partial, D.counter, st));
+        for (int j = 1; j <= i; ++j)
+          PM_CUDA(pm::gm_mgs(n, w, g(j), j < i ? g(j + 1) : nullptr, gs + k + 2 + j,
+                             j < i ? gs + k + 3 + j : gs + 2 * k + 3, D.partial, D.counter,
+                             st));
+        h->launches += 1 + i;
+        PM_TRY(read(k + 2, k + 2));
+        for (int j = 1; j <= i; ++j) Hm(j, i) = Hm(j, i) + hs[k + 2 + j];
+        norm = std::sqrt(hs[2 * k + 3]);
+      }
+      Hm(i + 1, i) = norm;
+      if (norm != 0.0) {
+        PM_CUDA(pm::gm_scale(n, w, 1.0 / norm, st));
+        h->launches += 1;
+      }
+      for (int j = 1; j <= i - 1; ++j) {
+        const double aux1 = c[j - 1] * Hm(j, i) + sn[j - 1] * Hm(j + 1, i);
+        const double aux2 = -sn[j - 1] * Hm(j, i) + c[j - 1] * Hm(j + 1, i);
+        Hm(j, i) = aux1;
+        Hm(j + 1, i) = aux2;
+      }
+      double r;
+      sym_ortho2(Hm(i, i), Hm(i + 1, i), c[i - 1], sn[i - 1], r);
+      Hm(i, i) = r;
+      Hm(i + 1, i) = 0.0;
+      e[i] = -sn[i - 1] * e[i - 1];
+      e[i - 1] = c[i - 1] * e[i - 1];
+      if (!std::isfinite(e[i])) {
+        h->err = "GMRES(l): breakdown (non-finite Givens rotation) after " +
+                 std::to_string(nit) + " iterations";
+        *nit_out = nit;
+        return PM_E_NOCONV;
+      }
+      if (std::fabs(e[i]) <= econv) break;
+    }
+    // R y = e (Iters.f:1575-1585), then x += sum_j y_j g_j
+    for (int j = 1; j <= ni; ++j) y[j - 1] = e[j - 1];
+    for (int j = ni; j >= 2; --j) {
+      y[j - 1] = y[j - 1] / Hm(j, j);
+      const double r = y[j - 1];
+      for (int i = 1; i <= j - 1; ++i) y[i - 1] = y[i - 1] - Hm(i, j) * r;
+    }
+    y[0] = y[0] / Hm(1, 1);
+    PM_CUDA(cudaMemcpyAsync(D.gm_y, y.data(), sizeof(double) * ni, cudaMemcpyHostToDevice, st));
+    PM_CUDA(pm::gm_update(n, x, G, D.gm_y, ni, st));
+    h->launches += 1;
+    if (h->debug)
+      fprintf(stderr, "gmres cycle %d: %d its, |e| %.3e conv %.3e\n", l, nit, std::fabs(e[ni]),
+              econv);
+    if (std::fabs(e[ni]) <= econv) {
+      *nit_out = nit;
+      PM_CUDA(cudaStreamSynchronize(st));
+      return PM_OK;
+    }
+  }
+  *nit_out = nit;
+  if (e[0] == 0.0) return PM_OK;
+  h->err = "GMRES(l): no convergence reached after " + std::to_string(maxit) + " cycles (" +
+           std::to_string(nit) + " iterations, nkrylov " + std::to_string(k) + ")";
+  return PM_E_NOCONV;
+}
+
 // One Krylov solve of K x = b on the device (solv_pm, Solv.f:27-780).
 //
 // comp = false: the reference's FP64 iteration on the FP64 panels.
@@ -480,6 +644,14 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       }
       --nrestart;
     }
+  } else if (solver == 2) {
+    if (comp) {
+      h->err = "GMRES(l) (solver 2) runs on the FP64 operator (PM_FP64)";
+      return PM_E_ARG;
+    }
+    int nit = 0;
+    PM_TRY(gmres_run(h, d_b, V.x, tol, maxit, &nit, &final_target));
+    ks.iter = nit;
   } else if (solver == 11) {
     if (comp) {
       h->err = "rpsqmr (solver 11) runs on the FP64 operator (PM_FP64)";
@@ -500,17 +672,27 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       PM_TRY(read_scalars(h, &ks));
       if (ks.conv_flag) break;
     }
+    if (ks.conv_flag == 2) {
+      // Solv.f:765: rpsqmr reached maxit; GMRES(l) from x = 0
+      const int its = ks.iter;
+      int nit = 0;
+      if (h->debug) fprintf(stderr, "rpsqmr: maxit reached, switching to GMRES(l)\n");
+      const int st2 = gmres_run(h, d_b, V.x, tol, maxit, &nit, &final_target);
+      if (st2 != PM_OK) {
+        if (info) info->iters = its + nit;
+        return st2;
+      }
+      ks.iter = its + nit;
+      ks.conv_flag = 1;
+    }
     if (ks.conv_flag != 1) {
-      h->err = ks.conv_flag == 3
-                   ? "rpsqmr: breakdown (sigma or rho zero, or non-finite) after " +
-                         std::to_string(ks.iter) + " iterations"
-                   : "rpsqmr: no convergence reached after " + std::to_string(ks.iter) +
-                         " iterations (the reference switches to GMRES(l) here)";
+      h->err = "rpsqmr: breakdown (sigma or rho zero, or non-finite) after " +
+               std::to_string(ks.iter) + " iterations";
       if (info) info->iters = ks.iter;
       return PM_E_NOCONV;
     }
   } else {
-    h->err = "solver must be 1 (pcg), 7 (minres) or 11 (rpsqmr)";
+    h->err = "solver must be 1 (pcg), 2 (gmres), 7 (minres) or 11 (rpsqmr)";
     return PM_E_ARG;
   }
   PM_CUDA(cudaEventRecord(e1, h->stream));
@@ -998,7 +1180,8 @@ void free_all(Handle* h) {
   pm::Dev& D = h->D;
   pm::Panels& P = h->P;
   void* ptrs[] = {D.ix, D.eq, D.x, D.mat, D.slot, D.color_elems, D.eload, D.eloadp, D.nload,
-                  D.load, D.fload, D.dofkind, D.fnno, D.u, D.u0, D.dp, D.poro, D.dporo, D.vcnt, D.f, D.b0, D.b, D.bst0,
+                  D.load, D.fload, D.dofkind, D.fnno, D.u, D.u0, D.dp, D.poro, D.dporo, D.vcnt, D.gm_basis, D.gm_scal,
+                  D.gm_y, D.f, D.b0, D.b, D.bst0,
                   D.ad, D.m, D.bx, D.by, D.rr, D.dx, D.xs, D.kv.x, D.kv.r, D.kv.z, D.kv.p, D.kv.q,
                   D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
@@ -1723,6 +1906,13 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   h->launches += 1;  // update_res
   h->timers[7] = (double)(h->launches - launches0);
   if (info) *info = loc;
+  return PM_OK;
+}
+
+int pm_set_nkrylov(pm_handle hh, int nkrylov) {
+  Handle* h = reinterpret_cast<Handle*>(hh);
+  if (!h || nkrylov < 1) return PM_E_ARG;
+  h->nkrylov = nkrylov;
   return PM_OK;
 }
 

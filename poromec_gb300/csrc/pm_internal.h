@@ -125,6 +125,9 @@ struct Dev {
   double *u = nullptr, *u0 = nullptr, *dp = nullptr, *f = nullptr;
   double *poro = nullptr, *dporo = nullptr;  // nodal porosity and its step change
   int32_t* vcnt = nullptr;                    // elements sharing each vertex node
+  double* gm_basis = nullptr;  // GMRES(l): (k+1) x neq Krylov basis, allocated on first use
+  double* gm_scal = nullptr;   // GMRES(l): per-step dot products (2k + 4)
+  double* gm_y = nullptr;      // GMRES(l): the cycle's coefficients (k)
   double *b0 = nullptr, *b = nullptr, *bst0 = nullptr;
   double *ad = nullptr, *m = nullptr;
   double *bx = nullptr, *by = nullptr;   // staging vectors for host calls
@@ -149,6 +152,8 @@ struct Handle {
   double inner_tol = 1.0e-5;   // inner tolerance of the FP32 refinement sweeps
                                // (and of a compensated MINRES cycle)
   double cycle_conv = 0.0;     // the current compensated MINRES cycle's target
+  int nkrylov = 150;           // GMRES(l) basis size (ngram, Main.f:274)
+  int gm_alloc_k = 0;          // basis size of the allocated D.gm_basis
   bool debug = false;          // PM_DEBUG set: solver progress on stderr
   std::vector<int32_t> color_ptr;
   std::vector<int32_t> h_eq;       // (ndf, nnode)

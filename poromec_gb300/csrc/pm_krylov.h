@@ -76,6 +76,18 @@ cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V,
 cudaError_t sqmr_iteration(const PanelView& P, const double* val64, int n, const double* m,
                            KrylovVecs& V, KrylovScalars* ks, double* partial,
                            unsigned* counter, cudaStream_t s);
+// GMRES(l) vector kernels (pm_gmres.cu)
+cudaError_t gm_resid(int n, const double* b, const double* ax, const double* m, double* g1,
+                     double* out, double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t gm_scale(int n, double* g, double sc, cudaStream_t s);
+cudaError_t gm_first(int n, double* w, const double* m, const double* g1, double* out,
+                     double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t gm_mgs(int n, double* w, const double* gj, const double* gnext, const double* bin,
+                   double* out, double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t gm_dot(int n, const double* a, const double* b, double* out, double* partial,
+                   unsigned* counter, cudaStream_t s);
+cudaError_t gm_update(int n, double* x, const double* G, const double* y, int ni,
+                      cudaStream_t s);
 cudaError_t minres_conv(int n, const double* b, const double* m, KrylovScalars* ks,
                         double tol, double* partial, unsigned* counter, cudaStream_t s);
 // pair != nullptr also writes the FP32 pair of z0 (compensated iteration)

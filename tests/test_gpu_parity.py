@@ -164,6 +164,60 @@ def test_rpsqmr_matches_oracle(problems, precond):
         assert np.linalg.norm(b - m.matvec(x)) <= 1e2 * tol * np.linalg.norm(b)
 
 
+@pytest.mark.parametrize("precond", [2, 5])
+def test_gmres_matches_oracle(problems, precond):
+    """GMRES(l) (solver 2, gmres2 Iters.f:1411-1700) with the default basis of
+    150: GPU and oracle stop on the same test |e| <= tol |M b|.  The tetra10
+    problem with |1/ad| takes two cycles (a restart).  The column with |1/ad|
+    needs 77 cycles and is left to the oracle's own tests."""
+    tol = 1e-10
+    for i, pb in enumerate(problems):
+        if precond == 5 and i == 2:
+            continue
+        m, o = _pair(pb)
+        m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+        _, _, ad, al = m.get_csrd()
+        o.set_csrd_values(ad, al)
+        b = np.random.default_rng(8).standard_normal(m.neq)
+        x, info = m.solve(b, solver=2, precond=precond, tol=tol, maxit=200)
+        xo, io = o.solve(b, solver=2, precond=precond, tol=tol, maxit=200)
+        assert np.abs(x - xo).max() <= 1e4 * tol * np.abs(xo).max(), i
+        assert info.iters > 0 and abs(info.iters - io.iters) <= max(3, io.iters // 20), (
+            i, info.iters, io.iters)
+        mm = 1.0 / ad if precond == 2 else np.abs(1.0 / ad)
+        assert np.linalg.norm(mm * (b - m.matvec(x))) <= 10 * tol * np.linalg.norm(mm * b)
+
+
+def test_rpsqmr_falls_back_to_gmres_on_gpu(problems):
+    """Solv.f:765: rpsqmr stopped at maxit switches to GMRES(l) from x = 0
+    with maxit cycles; the iteration count covers both."""
+    tol = 1e-10
+    for pb in problems[2:]:
+        m, o = _pair(pb)
+        m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+        _, _, ad, al = m.get_csrd()
+        o.set_csrd_values(ad, al)
+        b = np.random.default_rng(8).standard_normal(m.neq)
+        x, info = m.solve(b, solver=11, precond=2, tol=tol, maxit=10)
+        xo, io = o.solve(b, solver=11, precond=2, tol=tol, maxit=10)
+        xg, ig = m.solve(b, solver=2, precond=2, tol=tol, maxit=10)
+        assert np.array_equal(x, xg)
+        assert info.iters == 10 + ig.iters
+        assert np.abs(x - xo).max() <= 1e4 * tol * np.abs(xo).max()
+
+
+def test_gmres_steps_match_oracle():
+    pb = meshgen.column_problem()
+    m, o = _pair(pb)
+    for k in range(3):
+        m.step(maxnlit=2, stop_crit=1, solver=2, precond=2, solvtol=1e-10, maxit=200)
+        o.step(maxnlit=2, stop_crit=1, solver=2, precond=2, solvtol=1e-10, maxit=200)
+    u, _, _ = m.get_state()
+    uo, _, _ = o.get_state()
+    for sl in (slice(0, 3), slice(3, 4)):
+        assert np.abs(u[:, sl] - uo[:, sl]).max() <= 1e-8 * np.abs(uo[:, sl]).max()
+
+
 def test_rpsqmr_step_matches_oracle():
     """Steps of the consolidation column with the reference's default solver."""
     pb = meshgen.column_problem()
