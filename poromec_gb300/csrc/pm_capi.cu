@@ -828,6 +828,10 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   }
   const pm::PanelView P = h->P.view();
   PM_CUDA(cudaMemsetAsync(h->D.kv32.c, 0, sizeof(float2) * std::max(h->neq, 1), s));
+  // the PCG form (product fused with p.Ap), as the solver runs it: it writes
+  // only ks->pq and ks->alpha, which every solver's init sets again
+  PM_CUDA(cudaMemsetAsync(h->D.ks, 0, sizeof(pm::KrylovScalars), s));
+  constexpr int kReps = 5;
   float best = 0.f;
   int best_c = 1;
   for (int c : pm::kCfShapes) {
@@ -835,19 +839,24 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
     // memory, and not for batches (it does not skip converged instances)
     if (c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) continue;
     const pm::CompVals C = h->P.comp(c);
-    PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
+    auto run = [&]() {
+      return h->ninst > 0 ? pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s)
+                          : pm::spmvc_pcg(P, C, h->D.kv32.c, h->D.dx, h->D.xs, h->D.ks,
+                                          h->D.partial, h->D.counter, s);
+    };
+    PM_CUDA(run());
     PM_CUDA(cudaEventRecord(h->ev[0], s));
-    for (int k = 0; k < 3; ++k) PM_CUDA(pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s));
+    for (int k = 0; k < kReps; ++k) PM_CUDA(run());
     PM_CUDA(cudaEventRecord(h->ev[1], s));
     PM_CUDA(cudaEventSynchronize(h->ev[1]));
     float ms = 0.f;
     PM_CUDA(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
-    if (h->debug) fprintf(stderr, "spmv autotune: shape %2d  %.4f ms\n", c, ms / 3);
+    if (h->debug) fprintf(stderr, "spmv autotune: shape %2d  %.4f ms\n", c, ms / kReps);
     if (c == pm::kCfShapes[0] || ms < best) {
       best = ms;
       best_c = c;
     }
-    h->launches += 4;
+    h->launches += 1 + kReps;
   }
   h->shape = best_c;
   return PM_OK;

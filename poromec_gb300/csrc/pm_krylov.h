@@ -144,6 +144,10 @@ int ca_smem_bytes(int rec_max, int warps);
 cudaError_t ca_configure(int rec_max, int* warps, int* grid);
 cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s);
 cudaError_t spmvc(const PanelView& P, CompVals C, const float2* xp, double* y, cudaStream_t s);
+// the PCG form of the compensated product: y = A x and ks->alpha = ks->d / (y . xd)
+cudaError_t spmvc_pcg(const PanelView& P, CompVals C, const float2* xp, double* y,
+                      const double* xd, KrylovScalars* ks, double* partial, unsigned* counter,
+                      cudaStream_t s);
 cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,
                       KrylovVecs32& V32, KrylovScalars* ks, double tol, double conv_abs,
                       int maxit, double* partial, unsigned* counter, cudaStream_t s);

@@ -1458,6 +1458,13 @@ cudaError_t spmvc(const PanelView& P, CompVals C, const float2* xp, double* y, c
   return cudaGetLastError();
 }
 
+cudaError_t spmvc_pcg(const PanelView& P, CompVals C, const float2* xp, double* y,
+                      const double* xd, KrylovScalars* ks, double* partial, unsigned* counter,
+                      cudaStream_t s) {
+  launch_spmv_cf<1>(P, C, xp, y, xd, ks, partial, counter, s);
+  return cudaGetLastError();
+}
+
 cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,
                       KrylovVecs32& V32, KrylovScalars* ks, double tol, double conv_abs,
                       int maxit, double* partial, unsigned* counter, cudaStream_t s) {
