@@ -263,6 +263,45 @@ int pm_adjoint_grad_dev(pm_handle h, const double* d_lam, const double* d_un,
  * [6] Krylov iterations of the last solve, [7] kernels launched by the step. */
 int pm_get_timers(pm_handle h, double* t, int n);
 
+/* ---- input decks ---------------------------------------------------------
+ * pm_deck_read parses a deck of the reference: the macro program of Main.f
+ * (config, pcg / solver, gravity, mesh, setpnode, maxnlit / nl, dt, loop,
+ * solv, next, pnup, pnsf, pgeo, stop) and the mesh macro of rdat_pm
+ * (Rdata.f:1-1037: parameters, materials, fmaterials, hexa8 / tetra4 /
+ * hexa20 / tetra10, coordinates, constrainpmec, nodalforces, elmtloads,
+ * elmtpresloads, nodalloads, loads, initialpres, initialdisp, initialstress,
+ * hydrostatic, hydrostress, insert, return, end).  Linear elements with
+ * maxno 20 / 10 become hexa20 / tetra10 by mk_elconn_quad_v1
+ * (Adjacency.f:583-700), with the restraints, forces and initial stresses of
+ * the mid-side nodes from their edge's vertices (Rdata.f:2337-2544).  Older
+ * decks (element codes 7 / 6, "pcg", "maxnlit", inline type-40 loads) are
+ * read too.  Files named in the deck are relative to its directory.  On
+ * failure pm_deck_error() gives the message with file and line. */
+typedef struct pm_deck_s* pm_deck;
+int pm_deck_read(const char* path, pm_deck* d);
+const char* pm_deck_error(void);
+void pm_deck_free(pm_deck d);
+/* Scalars by name: nnode nnodev numel numat nen nenv nloads maxt fstress0
+ * mk_quad, the settings in force at the first solv (solver precond maxit
+ * solvtol maxnlit tol stop_crit nkrylov dt gravity_x gravity_y gravity_z),
+ * nprint, nops, unknown_macros. */
+int pm_deck_value(pm_deck d, const char* name, double* v);
+/* Arrays owned by the deck, in the layouts of pm_mesh_create / pm_set_loads:
+ * int32 ix id nload eload eloadp fnno load print_nodes; double e x f u0 tx0
+ * fload (u0 after boundc and bound_nodalloads; tx0(6, nnode)). */
+int pm_deck_int_array(pm_deck d, const char* name, const int32_t** p, int64_t* n);
+int pm_deck_real_array(pm_deck d, const char* name, const double** p, int64_t* n);
+/* A handle with the deck's mesh, loads, gravity, dt, initial state and
+ * initial stress. */
+int pm_deck_create(pm_deck d, pm_handle* h);
+/* Runs the macro program on h (from pm_deck_create): solv steps with the
+ * settings in force, pnup / pnsf writing <prefix>_<up|stress|stressE|stressB|
+ * flux|poro>_node_<n>.txt for the setpnode nodes (printnode, Pdata.f:733-790;
+ * pnsf adds the initial stress as Main.f does).  format 0 writes printnode's
+ * (i9,10e18.10) rows; format 1 the column layout of the golden runs shipped
+ * with the reference (i9, f30.6, f30.10 ...).  *nsteps = steps run. */
+int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nsteps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,15 @@ def load(path=None):
     lib.pm_stress.argtypes = [c_p] * 5
     lib.pm_get_porosity.argtypes = [c_p, c_p]
     lib.pm_set_nkrylov.argtypes = [c_p, c_i]
+    lib.pm_deck_read.argtypes = [ctypes.c_char_p, c_p]
+    lib.pm_deck_error.restype = ctypes.c_char_p
+    lib.pm_deck_free.argtypes = [c_p]
+    lib.pm_deck_free.restype = None
+    lib.pm_deck_value.argtypes = [c_p, ctypes.c_char_p, c_p]
+    lib.pm_deck_int_array.argtypes = [c_p, ctypes.c_char_p, c_p, c_p]
+    lib.pm_deck_real_array.argtypes = [c_p, ctypes.c_char_p, c_p, c_p]
+    lib.pm_deck_create.argtypes = [c_p, c_p]
+    lib.pm_deck_run.argtypes = [c_p, c_p, ctypes.c_char_p, c_i, c_p]
     lib.pm_set_porosity.argtypes = [c_p, c_p]
     lib.pm_stress_dev.argtypes = [c_p] * 6
     lib.pm_adjoint_apply_dev.argtypes = [c_p] * 5
@@ -152,6 +161,21 @@ class Mesh:
         self.lib.pm_get_sizes(h, ctypes.byref(neq), ctypes.byref(nad), ctypes.byref(nc),
                               ctypes.byref(nnz))
         self.neq, self.nad, self.numcolors, self.nnz_panel = neq.value, nad.value, nc.value, nnz.value
+
+    @classmethod
+    def adopt(cls, h, nnode, numel, nen, nenv):
+        """A Mesh around a handle created elsewhere in the library
+        (pm_deck_create); it is destroyed with the Mesh."""
+        m = cls.__new__(cls)
+        m.lib = load()
+        m.nnode, m.numel, m.nen, m.nenv = int(nnode), int(numel), int(nen), int(nenv)
+        m.ninst = 0
+        m.h = h
+        neq, nad, nc, nnz = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_int64()
+        m.lib.pm_get_sizes(h, ctypes.byref(neq), ctypes.byref(nad), ctypes.byref(nc),
+                           ctypes.byref(nnz))
+        m.neq, m.nad, m.numcolors, m.nnz_panel = neq.value, nad.value, nc.value, nnz.value
+        return m
 
     # ------------------------------------------------------------------
     def _check(self, st, what):

@@ -12,6 +12,7 @@
 #include <type_traits>
 
 #include "pm_internal.h"
+#include "pm_loads.h"
 
 using pm::Handle;
 
@@ -34,51 +35,6 @@ constexpr int kGraphIters = 16;  // Krylov iterations per captured graph
     if (st_ != PM_OK) return st_; \
   } while (0)
 
-__device__ double d_interp(const double* xs, const double* ys, double xi, int n) {
-  if (xi <= xs[0]) return ys[0];
-  if (xi >= xs[n - 1]) return ys[n - 1];
-  for (int i = 0; i < n - 1; ++i) {
-    const double x1 = xs[i], x2 = xs[i + 1], y1 = ys[i], y2 = ys[i + 1];
-    if (xi >= x1 && xi <= x2) return y1 + (y2 - y1) * (xi - x1) / (x2 - x1);
-  }
-  return 0.0;
-}
-
-// Scalar loads of tload (Pload.f:220-377) evaluated at a node.
-__device__ double d_nodal_load(const int32_t* load, const double* fload, int maxt, int nc,
-                               double t, const double* x, double u, double gmod) {
-  const int ty = load[3 * (nc - 1)];
-  const int nparc = load[3 * (nc - 1) + 1];
-  const int nt = load[3 * (nc - 1) + 2];
-  const double* F = fload + (size_t)maxt * PM_NFLOAD * (nc - 1);
-  auto col = [&](int k) { return F + (size_t)maxt * (k - 1); };
-  const double DOISPI = 6.283185307;
-  switch (ty) {
-    case 1: return F[0];
-    case 2: return F[0] + F[1] * t;
-    case 3: return (F[0] - u) * col(2)[0];
-    case 4:
-    case 5: {
-      double c = 0.0;
-      for (int i = 1; i <= nparc; ++i) {
-        const double a = col(i)[0], w = 1.0 / col(i)[1], t0 = col(i)[2];
-        const double ti = fmax(t - t0, 0.0);
-        c += a * (ty == 4 ? sin(DOISPI * w * ti) : cos(DOISPI * w * ti));
-      }
-      return c;
-    }
-    case 39:
-    case 41:
-    case 43: return d_interp(col(1), col(2), t, nt);
-    case 42: {
-      const double a = d_interp(col(1), col(2), t, nt), b = d_interp(col(1), col(3), t, nt);
-      const double w = d_interp(col(1), col(4), t, nt), t0 = d_interp(col(1), col(5), t, nt);
-      return t0 * (b + a * (w - x[2]) * gmod);
-    }
-    default: return 0.0;
-  }
-}
-
 // pload_pm (Pload.f:1-92): nodal loads and prescribed values at t.
 __global__ void k_pload(int nnode, const int32_t* __restrict__ eq, const int32_t* __restrict__ fnno,
                         const int32_t* __restrict__ nload, double* __restrict__ f,
@@ -91,7 +47,7 @@ __global__ void k_pload(int nnode, const int32_t* __restrict__ eq, const int32_t
     for (int j = 0; j < nj; ++j) {
       const size_t q = (size_t)4 * i + j;
       const int nc = nload ? nload[q] : 0;
-      if (nc > 0) f[q] = d_nodal_load(load, fload, maxt, nc, t, x + 3 * i, u[q], gmod);
+      if (nc > 0) f[q] = pm::nodal_load(load, fload, maxt, nc, t, x + 3 * i, u[q], gmod);
       const int k = eq[q];
       if (k > 0) b0[k - 1] = (j < 3) ? f[q] : -dt * f[q];
       else u[q] = f[q];

@@ -275,13 +275,31 @@ def convert(ref_root, kind, deck, prefix):
     return name, counts, nnode
 
 
+def check_library_reader(ref_root, kind, deck, prefix):
+    """The library's deck reader (pm_deck_read) on the shipped deck must give
+    the arrays of this script's restatement bit for bit."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from poromec_gb300.deck import Deck
+    fx = np.load(os.path.join(HERE, prefix + ".npz"))
+    pb = Deck(os.path.join(ref_root, "output", "poro_mec", "elastico", kind, deck)).problem()
+    for k in ("ix", "id", "fnno", "x", "e", "ie", "eload", "load", "fload", "u0"):
+        if pb[k].shape != fx[k].shape or not np.array_equal(pb[k], fx[k]):
+            raise SystemExit("library deck reader differs on %s: %s" % (deck, k))
+    if list(pb["print_nodes"]) != list(fx["hist_nodes"]):
+        raise SystemExit("library deck reader differs on %s: setpnode" % deck)
+    return True
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     for kind, deck, prefix in CASES:
         name, counts, nnode = convert(ref_root, kind, deck, prefix)
-        print("%-28s nnode %6d (log %s) neq %s nad %s" % (
+        checked = False
+        if not MISSING:
+            checked = check_library_reader(ref_root, kind, deck, prefix)
+        print("%-28s nnode %6d (log %s) neq %s nad %s  library reader %s" % (
             os.path.basename(name), nnode, counts.get("nnode"), counts.get("neq"),
-            counts.get("nad")))
+            counts.get("nad"), "identical" if checked else "skipped (deck incomplete)"))
 
 
 if __name__ == "__main__":

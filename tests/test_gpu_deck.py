@@ -1,0 +1,77 @@
+"""Decks run end to end on the GPU (pm_deck_run): the golden Terzaghi
+columns written back as decks in the shipped decks' syntax, their macro
+program (600 steps of solv / pnup / pnsf) run by the library, and the
+history files compared with the reference's printed histories.
+
+Both sides print 10 decimals in the golden layout, so the bar is one unit
+in the last printed digit plus the solver tolerance.  The tetra10 run pins
+u, p and the flux; its printed stresses come from an earlier tetra10 stress
+pass (tests/test_oracle_stress.py).
+"""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from deck_writer import write_linear_deck
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from poromec_gb300.deck import Deck, read_history  # noqa: E402
+
+GOLDEN_HEADERS = {"up": "DeslocAndPress", "stress": "stressTotal", "stressE": "stressE",
+                  "stressB": "stressBiot", "flux": "stressFlux"}
+
+
+@pytest.mark.parametrize("name,keys", [
+    ("exemplo1_mesh0_t2", ("up", "stress", "stressE", "stressB", "flux")),
+    ("exemplo1_mesh0_t2_tetra", ("up", "flux")),
+])
+def test_deck_run_matches_golden_histories(golden, tmp_path, name, keys):
+    fx = golden(name)
+    path = write_linear_deck(fx, str(tmp_path), name)
+    prefix = os.path.join(str(tmp_path), "out", name)
+    os.makedirs(os.path.dirname(prefix))
+    _, nsteps = Deck(path).run(prefix, fmt="golden")
+    assert nsteps == int(fx["nsteps"]) == 600
+    ref = {"up": fx["hist"], "stress": fx["hist_stress"], "stressE": fx["hist_stressE"],
+           "stressB": fx["hist_stressB"], "flux": fx["hist_flux"]}
+    for a, n in enumerate(fx["hist_nodes"]):
+        for k in keys:
+            fn = "%s_%s_node_%d.txt" % (prefix, k, n)
+            with open(fn) as fh:
+                head = fh.readline()
+            assert head == "# Variacao %s no tempo no ponto%9d\n" % (GOLDEN_HEADERS[k], n)
+            h = read_history(fn)
+            r = ref[k][a]
+            assert h.shape == r.shape, (k, h.shape, r.shape)
+            assert np.array_equal(h[:, 0], r[:, 0])                       # istep
+            assert np.abs(h[:, 1] - r[:, 1]).max() <= 1e-6                # t, 6 decimals
+            assert np.abs(h[:, 2:] - r[:, 2:]).max() <= 1.5e-10, (k, n)
+        assert os.path.exists("%s_poro_node_%d.txt" % (prefix, n))
+
+
+def test_printnode_layout(golden, tmp_path):
+    """pnup / pnsf in printnode's (i9,10e18.10) rows (Pdata.f:760)."""
+    fx = golden("exemplo1_mesh0_t2")
+    path = write_linear_deck(fx, str(tmp_path), "t", nsteps=3)
+    prefix = os.path.join(str(tmp_path), "t")
+    Deck(path).run(prefix, fmt="printnode")
+    for k, ncol in (("up", 4), ("stress", 6), ("flux", 3), ("poro", 1)):
+        with open("%s_%s_node_1.txt" % (prefix, k)) as fh:
+            lines = fh.read().splitlines()
+        assert lines[0].startswith("# Variacao ")
+        assert len(lines) == 5
+        for ln in lines[1:]:
+            assert len(ln) == 9 + 18 * (ncol + 1)
+            fields = [ln[9 + 18 * j:9 + 18 * (j + 1)] for j in range(ncol + 1)]
+            for f in fields:
+                assert re.fullmatch(r" *-?0\.\d{10}E[+-]\d{2}", f), f
+    h = read_history("%s_up_node_1.txt" % prefix)
+    r = fx["hist"][0][:4]
+    assert np.abs(h[:, 2:] - r[:, 2:]).max() <= 1.5e-10
