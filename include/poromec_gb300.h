@@ -297,10 +297,23 @@ int pm_deck_create(pm_deck d, pm_handle* h);
 /* Runs the macro program on h (from pm_deck_create): solv steps with the
  * settings in force, pnup / pnsf writing <prefix>_<up|stress|stressE|stressB|
  * flux|poro>_node_<n>.txt for the setpnode nodes (printnode, Pdata.f:733-790;
- * pnsf adds the initial stress as Main.f does).  format 0 writes printnode's
+ * pnsf adds the initial stress as Main.f does), pgeo and pres writing the VTK
+ * files of pm_deck_write_geo / pm_deck_write_res (pres with every field).  format 0 writes printnode's
  * (i9,10e18.10) rows; format 1 the column layout of the golden runs shipped
  * with the reference (i9, f30.6, f30.10 ...).  *nsteps = steps run. */
 int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nsteps);
+/* Legacy ASCII VTK (Vtk.f, Write_vtk.f).  pm_deck_write_geo: the mesh as
+ * read (write_mesh_geo_pm, the pgeo macro), <prefix>_bc.vtk: node ids and one
+ * field per node macro of the deck (restraint flags, forces, nodal loads,
+ * initial pressure, initial stress) in read order, cell materials, ids and
+ * element loads; quad = 0 writes the vertex mesh of a linear deck.
+ * pm_deck_write_res: the state of h (write_mesh_res_pm, the pres macro),
+ * <prefix>_istep_<istep>.vtk: desloc, pressao, and by the bits of fields
+ * 1 deltaPressao, 2 totalStress, 4 terzaghiStress, 8 BiotStress,
+ * 16 darcyFlux, 32 porosity; mid-side pressures are the edge averages. */
+int pm_deck_write_geo(pm_deck d, const char* prefix, int quad);
+int pm_deck_write_res(pm_deck d, pm_handle h, const char* prefix, int istep, double t, int quad,
+                      int fields);
 
 #ifdef __cplusplus
 }

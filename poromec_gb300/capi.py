@@ -98,6 +98,8 @@ def load(path=None):
     lib.pm_deck_real_array.argtypes = [c_p, ctypes.c_char_p, c_p, c_p]
     lib.pm_deck_create.argtypes = [c_p, c_p]
     lib.pm_deck_run.argtypes = [c_p, c_p, ctypes.c_char_p, c_i, c_p]
+    lib.pm_deck_write_geo.argtypes = [c_p, ctypes.c_char_p, c_i]
+    lib.pm_deck_write_res.argtypes = [c_p, c_p, ctypes.c_char_p, c_i, c_d, c_i, c_i]
     lib.pm_set_porosity.argtypes = [c_p, c_p]
     lib.pm_stress_dev.argtypes = [c_p] * 6
     lib.pm_adjoint_apply_dev.argtypes = [c_p] * 5

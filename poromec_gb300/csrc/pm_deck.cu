@@ -46,7 +46,7 @@ const int kTetraEdges[6][3] = {{1, 2, 5}, {1, 3, 6}, {1, 4, 7},
                                {2, 3, 8}, {3, 4, 9}, {4, 2, 10}};
 
 enum OpKind { OP_SOLV, OP_PNUP, OP_PNSF, OP_LOOP, OP_NEXT, OP_DT, OP_NL, OP_SOLVER,
-              OP_GRAVITY, OP_PGEO, OP_STOP };
+              OP_GRAVITY, OP_PGEO, OP_PRES, OP_STOP };
 
 struct Settings {
   int solver = 11, precond = 2, maxit = 50000, maxnlit = 500, stop_crit = 2, nkrylov = 150;
@@ -181,6 +181,7 @@ struct pm_deck_s {
   Settings run0;  // settings in force at the first solv (at the end without one)
   bool have_run0 = false;
   std::vector<Op> prog;
+  std::vector<std::string> node_macros, cell_macros;  // fields of the geometry file, read order
   int nunknown = 0;
 };
 
@@ -628,6 +629,11 @@ bool read_mesh(Reader& r, pm_deck_s* d, const Settings& s) {
   };
   while (r.next(w)) {
     const std::string& m = w[0];
+    for (const char* k : {"constrainpmec", "constraindisp", "nodalforces", "nodalloads",
+                          "initialpres", "initialstress"})
+      if (m == k) d->node_macros.push_back(m);
+    for (const char* k : {"elmtloads", "elmtpresloads"})
+      if (m == k) d->cell_macros.push_back(m);
     if (m == "end") {
       finish_loads(d, tabs);
       return finish_mesh(r, d);
@@ -849,6 +855,8 @@ bool parse(Reader& r, pm_deck_s* d) {
       d->prog.push_back(Op{OP_PNSF});
     } else if (m == "pgeo") {
       d->prog.push_back(Op{OP_PGEO});
+    } else if (m == "pres") {
+      d->prog.push_back(Op{OP_PRES});
     } else if (m == "stop") {
       d->prog.push_back(Op{OP_STOP});
       break;
@@ -920,6 +928,240 @@ struct Printer {
     return PM_OK;
   }
 };
+
+// ---- legacy ASCII VTK (Vtk.f, Write_vtk.f) ----------------------------------
+// Fortran Ew.d / Ew.dEe edit descriptors: 0.d1..dd mantissa, the exponent
+// with e digits (2 by default, the form without 'E' past 99).
+std::string fortran_e(double v, int w, int dd, int edig) {
+  char b[64];
+  if (!std::isfinite(v)) {
+    std::snprintf(b, sizeof b, "%*s", w, std::isnan(v) ? "NaN" : v > 0 ? "Infinity" : "-Infinity");
+    return b;
+  }
+  int ex = 0;
+  std::string digits(dd, '0');
+  bool neg = std::signbit(v) && v != 0.0;
+  if (v != 0.0) {
+    char m[64];
+    std::snprintf(m, sizeof m, "%.*E", dd - 1, v);
+    const char* p = m;
+    if (*p == '-') ++p;
+    digits.clear();
+    for (; *p && *p != 'E'; ++p)
+      if (*p != '.') digits += *p;
+    ex = std::atoi(p + 1) + 1;
+  }
+  char e[16];
+  if (std::abs(ex) < (edig == 2 ? 100 : 1000))
+    std::snprintf(e, sizeof e, "E%c%0*d", ex < 0 ? '-' : '+', edig, std::abs(ex));
+  else
+    std::snprintf(e, sizeof e, "%c%0*d", ex < 0 ? '-' : '+', edig + 1, std::abs(ex));
+  std::snprintf(b, sizeof b, "%*s", w,
+                ((neg ? "-" : "") + std::string("0.") + digits + e).c_str());
+  return b;
+}
+
+void vtk_head(FILE* f, const char* title, bool time, double t, int istep) {
+  std::fprintf(f, "# vtk DataFile Version 3.0\n%-30s\nASCII\nDATASET UNSTRUCTURED_GRID\n",
+               title);
+  if (time)
+    std::fprintf(f,
+                 "FIELD FieldData 4\nTIME_S 1 1 double\n%16.6f\nTIME_H 1 1 double\n%16.6f\n"
+                 "TIME_D 1 1 double\n%16.6f\nCYCLE 1 1 int\n%9d\n",
+                 t, t / 3600.0, t / (24.0 * 3600.0), istep);
+}
+
+// coor_vtk / elm_vtk: quad = all nodes and hexa20 / tetra10 cells (VTK types
+// 25 / 24 in the node orders of elm_vtk), else the vertex mesh
+int vtk_mesh(FILE* f, const pm_deck_s* d, bool quad, int* npts) {
+  const int nen = d->nen, nenv = d->nenv;
+  const bool vert = !quad && d->mk_quad;
+  const int np = vert ? d->nnodev : d->nnode;
+  *npts = np;
+  std::fprintf(f, "POINTS %10d double\n", np);
+  for (int i = 0; i < np; ++i) {
+    for (int k = 0; k < 3; ++k) std::fputs(fortran_e(d->x[(size_t)3 * i + k], 15, 5, 2).c_str(), f);
+    std::fputc('\n', f);
+  }
+  static const int hexa20_vtk[20] = {5, 6, 7, 8, 1, 2, 3, 4, 13, 14,
+                                     15, 16, 9, 10, 11, 12, 17, 18, 19, 20};
+  static const int tetra10_vtk[10] = {1, 2, 3, 4, 5, 8, 6, 7, 10, 9};
+  const int nno = quad ? nen : nenv;
+  std::fprintf(f, "CELLS %10d%10d\n", d->numel, d->numel * (nno + 1));
+  for (int el = 0; el < d->numel; ++el) {
+    const int32_t* nd = &d->ix[(size_t)(nen + 1) * el];
+    std::fprintf(f, "%10d", nno);
+    for (int k = 0; k < nno; ++k) {
+      const int slot = !quad ? k : nen == 20 ? hexa20_vtk[k] - 1 : tetra10_vtk[k] - 1;
+      std::fprintf(f, "%10d", nd[slot] - 1);
+    }
+    std::fputc('\n', f);
+  }
+  const int type = quad ? (nen == 20 ? 25 : 24) : (nen == 20 ? 12 : 10);
+  std::fprintf(f, "CELL_TYPES %10d\n", d->numel);
+  for (int el = 0; el < d->numel; ++el) std::fprintf(f, "%3d\n", type);
+  return PM_OK;
+}
+
+void vtk_point_int(FILE* f, const char* name, const int32_t* a, int np, int gdl) {
+  std::fprintf(f, "SCALARS %-15s %-8s %3d\nLOOKUP_TABLE default\n", name, "int", gdl);
+  for (int i = 0; i < np; ++i) {
+    for (int j = 0; j < gdl; ++j) std::fprintf(f, "%10d", a[(size_t)gdl * i + j]);
+    std::fputc('\n', f);
+  }
+}
+
+void vtk_point_real(FILE* f, const char* name, const double* a, int np, int gdl, int stride) {
+  std::fprintf(f, "SCALARS %-15s %-8s %3d\nLOOKUP_TABLE default\n", name, "double", gdl);
+  for (int i = 0; i < np; ++i) {
+    for (int j = 0; j < gdl; ++j)
+      std::fputs(fortran_e(a[(size_t)stride * i + j], 15, 5, 3).c_str(), f);
+    std::fputc('\n', f);
+  }
+}
+
+void vtk_vectors(FILE* f, const char* name, const double* a, int np, int stride) {
+  std::fprintf(f, "VECTORS %-15s double\n", name);
+  for (int i = 0; i < np; ++i) {
+    for (int j = 0; j < 3; ++j)
+      std::fputs(fortran_e(a[(size_t)stride * i + j], 15, 5, 3).c_str(), f);
+    std::fputc('\n', f);
+  }
+}
+
+// make_full_tensor (Write_vtk.f:2310-2387): (xx, yy, zz, xy, yz, xz) -> 3 x 3
+void vtk_tensors(FILE* f, const char* name, const double* t, int np) {
+  std::fprintf(f, "TENSORS %-15s double\n", name);
+  static const int map[9] = {0, 3, 5, 3, 1, 4, 5, 4, 2};
+  for (int i = 0; i < np; ++i) {
+    for (int j = 0; j < 9; ++j)
+      std::fputs(fortran_e(t[(size_t)kNtn * i + map[j]], 15, 5, 3).c_str(), f);
+    std::fputc('\n', f);
+  }
+}
+
+void vtk_cell_int(FILE* f, const char* name, const int32_t* a, int n, int gdl) {
+  std::fprintf(f, " SCALARS %-15s int %11d\nLOOKUP_TABLE default\n", name, gdl);
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < gdl; ++j) std::fprintf(f, "%10d", a[(size_t)gdl * i + j]);
+    std::fputc('\n', f);
+  }
+}
+
+void vtk_cells_common(FILE* f, const pm_deck_s* d) {
+  std::fprintf(f, "CELL_DATA %9d\n", d->numel);
+  std::vector<int32_t> v(d->numel);
+  for (int el = 0; el < d->numel; ++el) v[el] = d->ix[(size_t)(d->nen + 1) * el + d->nen];
+  vtk_cell_int(f, "mat", v.data(), d->numel, 1);
+  for (int el = 0; el < d->numel; ++el) v[el] = el + 1;
+  vtk_cell_int(f, "elIdG", v.data(), d->numel, 1);
+}
+
+// mid-side values as the average of their edge's vertices (split_u_p,
+// mk_field_quad)
+void quad_fill(const pm_deck_s* d, std::vector<double>& a, int gdl) {
+  if (!d->mk_quad) return;
+  for_edges(d, [&](int p, int q, int m) {
+    for (int k = 0; k < gdl; ++k)
+      a[(size_t)gdl * m + k] = 0.5 * (a[(size_t)gdl * p + k] + a[(size_t)gdl * q + k]);
+  });
+}
+
+// write_mesh_geo_pm (Write_vtk.f:210-700): the mesh as read, <prefix>_bc.vtk
+int write_geo(const pm_deck_s* d, const std::string& prefix, bool quad) {
+  const std::string fn = prefix + "_bc.vtk";
+  FILE* f = std::fopen(fn.c_str(), "w");
+  if (!f) return PM_E_ARG;
+  vtk_head(f, "Geometria lida", false, 0.0, 0);
+  int np = 0;
+  vtk_mesh(f, d, quad, &np);
+  std::fprintf(f, "POINT_DATA %9d\n", np);
+  std::vector<int32_t> ids(np);
+  for (int i = 0; i < np; ++i) ids[i] = i + 1;
+  vtk_point_int(f, "noIdG", ids.data(), np, 1);
+  for (const std::string& m : d->node_macros) {
+    if (m == "constrainpmec" || m == "constraindisp") {
+      vtk_point_int(f, m.c_str(), d->id.data(), np, kNdf);
+    } else if (m == "nodalforces") {
+      vtk_point_real(f, "forces", d->f.data(), np, kNdf, kNdf);
+    } else if (m == "nodalloads") {
+      vtk_point_int(f, "nodalloads", d->nload.data(), np, kNdf);
+    } else if (m == "initialpres") {
+      std::vector<double> p(d->nnode);
+      for (int i = 0; i < d->nnode; ++i) p[i] = d->u0[(size_t)kNdf * i + 3];
+      if (quad) quad_fill(d, p, 1);
+      vtk_point_real(f, "initialpres", p.data(), np, 1, 1);
+    } else if (m == "initialstress") {
+      vtk_tensors(f, "initialstress", d->tx0.data(), np);
+    }
+  }
+  vtk_cells_common(f, d);
+  for (const std::string& m : d->cell_macros)
+    vtk_cell_int(f, m.c_str(), m == "elmtloads" ? d->eload.data() : d->eloadp.data(), d->numel, 7);
+  std::fclose(f);
+  return PM_OK;
+}
+
+// write_mesh_res_pm (Write_vtk.f:912-1399): <prefix>_istep_<n>.vtk
+int write_res(const pm_deck_s* d, pm_handle h, const std::string& prefix, int istep, double t,
+              bool quad, int fields) {
+  const int nn = d->nnode;
+  std::vector<double> u((size_t)kNdf * nn), dp(nn), poro(nn);
+  std::vector<double> tx((size_t)kNtn * nn), txb((size_t)kNtn * nn), txe((size_t)kNtn * nn),
+      fl((size_t)3 * nn);
+  int st;
+  if ((st = pm_get_state(h, u.data(), nullptr, dp.data())) != PM_OK) return st;
+  if ((fields & 0x1e) && (st = pm_stress(h, tx.data(), txb.data(), txe.data(), fl.data())) != PM_OK)
+    return st;
+  if ((fields & 0x20) && (st = pm_get_porosity(h, poro.data())) != PM_OK) return st;
+  if (d->fstress0 && (fields & 0x0e)) {
+    for (size_t q = 0; q < tx.size(); ++q) {
+      tx[q] += d->tx0[q];
+      txb[q] += d->tx0[q];
+    }
+    for (int i = 0; i < nn; ++i)
+      for (int k = 0; k < kNtn; ++k)
+        txe[(size_t)kNtn * i + k] = tx[(size_t)kNtn * i + k] + (k < 3 ? u[(size_t)kNdf * i + 3] : 0.0);
+  }
+  const std::string fn = prefix + "_istep_" + std::to_string(istep) + ".vtk";
+  FILE* f = std::fopen(fn.c_str(), "w");
+  if (!f) return PM_E_ARG;
+  vtk_head(f, "Malha poro mec", true, t, istep);
+  int np = 0;
+  vtk_mesh(f, d, quad, &np);
+  vtk_cells_common(f, d);
+  std::fprintf(f, "POINT_DATA %9d\n", np);
+  std::vector<int32_t> ids(np);
+  for (int i = 0; i < np; ++i) ids[i] = i + 1;
+  vtk_point_int(f, "noIdG", ids.data(), np, 1);
+  vtk_vectors(f, "desloc", u.data(), np, kNdf);
+  std::vector<double> p(nn);
+  for (int i = 0; i < nn; ++i) p[i] = u[(size_t)kNdf * i + 3];
+  if (quad) quad_fill(d, p, 1);
+  vtk_point_real(f, "pressao", p.data(), np, 1, 1);
+  if (fields & 0x01) {
+    if (quad) quad_fill(d, dp, 1);
+    vtk_point_real(f, "deltaPressao", dp.data(), np, 1, 1);
+  }
+  if (fields & 0x20) {
+    if (quad) quad_fill(d, poro, 1);
+    vtk_point_real(f, "porosity", poro.data(), np, 1, 1);
+  }
+  if (fields & 0x10) {
+    if (quad) quad_fill(d, fl, 3);
+    vtk_vectors(f, "darcyFlux", fl.data(), np, 3);
+  }
+  if (quad && (fields & 0x0e)) {
+    quad_fill(d, tx, kNtn);
+    quad_fill(d, txe, kNtn);
+    quad_fill(d, txb, kNtn);
+  }
+  if (fields & 0x02) vtk_tensors(f, "totalStress", tx.data(), np);
+  if (fields & 0x04) vtk_tensors(f, "terzaghiStress", txe.data(), np);
+  if (fields & 0x08) vtk_tensors(f, "BiotStress", txb.data(), np);
+  std::fclose(f);
+  return PM_OK;
+}
 
 }  // namespace
 
@@ -1104,6 +1346,10 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
         break;
       }
       case OP_PGEO:
+        if ((st = write_geo(d, prefix, false)) != PM_OK) return st;
+        break;
+      case OP_PRES:
+        if ((st = write_res(d, h, prefix, istep, t, true, 0x3f)) != PM_OK) return st;
         break;
       case OP_STOP:
         pc = d->prog.size();
@@ -1112,6 +1358,17 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
   }
   if (nsteps) *nsteps = istep;
   return PM_OK;
+}
+
+int pm_deck_write_geo(pm_deck d, const char* prefix, int quad) {
+  if (!d || !prefix) return PM_E_ARG;
+  return write_geo(d, prefix, quad != 0);
+}
+
+int pm_deck_write_res(pm_deck d, pm_handle h, const char* prefix, int istep, double t, int quad,
+                      int fields) {
+  if (!d || !h || !prefix) return PM_E_ARG;
+  return write_res(d, h, prefix, istep, t, quad != 0, fields);
 }
 
 }  // extern "C"

@@ -111,6 +111,23 @@ class Deck:
         return capi.Mesh.adopt(h, self.value("nnode"), self.value("numel"), self.value("nen"),
                                self.value("nenv"))
 
+    def write_geo(self, prefix, quad=False):
+        """<prefix>_bc.vtk: the mesh as read (the pgeo macro)."""
+        st = self.lib.pm_deck_write_geo(self.d, os.fspath(prefix).encode(), int(bool(quad)))
+        if st != 0:
+            raise DeckError("cannot write %s_bc.vtk" % prefix)
+        return os.fspath(prefix) + "_bc.vtk"
+
+    def write_res(self, mesh, prefix, istep, t, quad=True, fields=0x3F):
+        """<prefix>_istep_<istep>.vtk: the state of mesh (the pres macro);
+        fields bits: 1 deltaPressao, 2 totalStress, 4 terzaghiStress,
+        8 BiotStress, 16 darcyFlux, 32 porosity."""
+        st = self.lib.pm_deck_write_res(self.d, mesh.h, os.fspath(prefix).encode(), int(istep),
+                                        float(t), int(bool(quad)), int(fields))
+        if st != 0:
+            raise capi.PMError(st, "pm_deck_write_res")
+        return "%s_istep_%d.vtk" % (os.fspath(prefix), istep)
+
     def run(self, prefix, fmt="printnode", mesh=None):
         """Run the deck's macro program; history files go to <prefix>_*.txt.
         fmt 'printnode' writes the reference's (i9,10e18.10) rows, 'golden'
@@ -133,6 +150,77 @@ def read_history(path):
                 continue
             rows.append([float(v.replace("D", "E")) for v in line.split()])
     return np.array(rows)
+
+
+def read_vtk(path):
+    """Arrays of a legacy ASCII VTK unstructured grid (the reference's
+    _bc.vtk / _istep_N.vtk files, or ours): dict with points (n, 3), cells
+    (list of node-index arrays), cell_types, point_data and cell_data
+    ({name: (n, ncomp) array}) and the FieldData values (TIME_S, CYCLE ...)."""
+    with open(path, errors="replace") as fh:
+        lines = fh.read().splitlines()
+    toks = []
+    for ln in lines[4:]:
+        toks.extend(ln.split())
+    out = {"point_data": {}, "cell_data": {}, "field": {}}
+    i, section = 0, None
+
+    def nums(count, conv=float):
+        nonlocal i
+        v = [conv(t.replace("D", "E")) for t in toks[i:i + count]]
+        i += count
+        return v
+
+    while i < len(toks):
+        key = toks[i]
+        if key == "FIELD":
+            nf = int(toks[i + 2])
+            i += 3
+            for _ in range(nf):
+                name, nc, nt = toks[i], int(toks[i + 1]), int(toks[i + 2])
+                i += 4
+                out["field"][name] = nums(nc * nt)
+        elif key == "POINTS":
+            n = int(toks[i + 1])
+            i += 3
+            out["points"] = np.array(nums(3 * n)).reshape(n, 3)
+        elif key == "CELLS":
+            n, size = int(toks[i + 1]), int(toks[i + 2])
+            i += 3
+            flat = nums(size, int)
+            cells, k = [], 0
+            for _ in range(n):
+                cells.append(np.array(flat[k + 1:k + 1 + flat[k]]))
+                k += 1 + flat[k]
+            out["cells"] = cells
+        elif key == "CELL_TYPES":
+            n = int(toks[i + 1])
+            i += 2
+            out["cell_types"] = np.array(nums(n, int))
+        elif key in ("POINT_DATA", "CELL_DATA"):
+            section = "point_data" if key == "POINT_DATA" else "cell_data"
+            out[section + "_n"] = int(toks[i + 1])
+            i += 2
+        elif key == "SCALARS":
+            name, typ = toks[i + 1], toks[i + 2]
+            nc = 1
+            j = i + 3
+            if j < len(toks) and toks[j].isdigit():
+                nc = int(toks[j])
+                j += 1
+            assert toks[j] == "LOOKUP_TABLE"
+            i = j + 2
+            n = out[section + "_n"]
+            conv = int if typ == "int" else float
+            out[section][name] = np.array(nums(n * nc, conv)).reshape(n, nc)
+        elif key in ("VECTORS", "TENSORS"):
+            name = toks[i + 1]
+            i += 3
+            n, nc = out[section + "_n"], 3 if key == "VECTORS" else 9
+            out[section][name] = np.array(nums(n * nc)).reshape(n, nc)
+        else:
+            raise ValueError("unexpected VTK token %r in %s" % (key, path))
+    return out
 
 
 def main(argv=None):

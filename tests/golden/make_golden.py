@@ -258,6 +258,20 @@ def convert(ref_root, kind, deck, prefix):
                 rows[n] = read_history(pth)
         if rows and sorted(rows) == sorted(hist):
             extra[key] = np.stack([rows[n] for n in sorted(rows)])
+    # the pgeo geometry file of the run (legacy VTK): mesh and input fields
+    vtk = {}
+    bc = os.path.join(ddir, prefix + "_bc.vtk")
+    if os.path.exists(bc):
+        sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+        from poromec_gb300.deck import read_vtk
+        g = read_vtk(bc)
+        vtk["vtk_points"] = g["points"]
+        vtk["vtk_cells"] = np.stack(g["cells"])
+        vtk["vtk_types"] = g["cell_types"]
+        for k, v in g["point_data"].items():
+            vtk["vtkp_" + k] = v
+        for k, v in g["cell_data"].items():
+            vtk["vtkc_" + k] = v
     counts = read_counts(os.path.join(ddir, prefix + "_t_1.txt"))
     its = read_log(os.path.join(ddir, prefix + "_log_1.txt"))
     tol = d["solver_tol"] if d["solver_tol"] != 0.0 else 2.0 ** -53  # smachn
@@ -269,7 +283,7 @@ def convert(ref_root, kind, deck, prefix):
                maxit=d["maxit"], reord=int(d["reord"]), hist_nodes=hnodes,
                hist=np.stack([hist[n] for n in hnodes]) if len(hnodes) else np.zeros(0),
                pcg_iters=its, neq_ref=counts.get("neq", -1), nad_ref=counts.get("nad", -1),
-               nnode_ref=counts.get("nnode", -1), complete=int(not MISSING), **extra)
+               nnode_ref=counts.get("nnode", -1), complete=int(not MISSING), **extra, **vtk)
     name = os.path.join(HERE, prefix + ".npz")
     np.savez_compressed(name, **out)
     return name, counts, nnode

@@ -20,7 +20,7 @@ import pytest
 from deck_writer import write_linear_deck
 
 pytest.importorskip("ctypes")
-from poromec_gb300.deck import Deck, DeckError  # noqa: E402
+from poromec_gb300.deck import Deck, DeckError, read_vtk  # noqa: E402
 
 ARRAYS = ["ix", "id", "fnno", "x", "e", "ie", "eload", "load", "u0", "fload"]
 
@@ -207,3 +207,40 @@ def test_errors_name_file_and_line(tmp_path, text, msg):
     assert msg in str(e.value)
     if "not found" not in msg and "without 'next'" not in msg:
         assert "bad.dat:" in str(e.value)
+
+
+@pytest.mark.parametrize("name", ["exemplo1_mesh0_t2", "solo1", "solo_cilindro_hexa_1",
+                                  "solo_cilindro_tetra_1"])
+def test_geometry_vtk_matches_the_golden_file(golden, tmp_path, name):
+    """pgeo (write_mesh_geo_pm, Write_vtk.f:210-700) against the _bc.vtk the
+    reference wrote for the same deck (its fields stored in the fixture by
+    make_golden.py): the vertex mesh, node ids, initial pressures and
+    restraint flags, cell materials, ids and element loads.  Values are
+    printed with 5 digits (e15.5) by both writers."""
+    fx = golden(name)
+    d = Deck(write_linear_deck(fx, str(tmp_path), name))
+    g = read_vtk(d.write_geo(os.path.join(str(tmp_path), name)))
+    assert np.array_equal(g["points"], fx["vtk_points"])
+    assert np.array_equal(np.stack(g["cells"]), fx["vtk_cells"])
+    assert np.array_equal(g["cell_types"], fx["vtk_types"])
+    for k in fx:
+        if k.startswith("vtkp_"):
+            assert np.array_equal(g["point_data"][k[5:]], fx[k]), k
+        elif k.startswith("vtkc_"):
+            assert np.array_equal(g["cell_data"][k[5:]], fx[k]), k
+
+
+def test_quadratic_geometry_vtk(golden, tmp_path):
+    fx = golden("exemplo1_mesh0_t2")
+    d = Deck(write_linear_deck(fx, str(tmp_path), "q"))
+    g = read_vtk(d.write_geo(os.path.join(str(tmp_path), "q"), quad=True))
+    assert g["points"].shape == (int(fx["nnode"]), 3)
+    assert set(g["cell_types"]) == {25}
+    # VTK quadratic hexahedron order (elm_vtk): top face first, then its edges
+    ix = fx["ix"][0]
+    order = [5, 6, 7, 8, 1, 2, 3, 4, 13, 14, 15, 16, 9, 10, 11, 12, 17, 18, 19, 20]
+    assert list(g["cells"][0]) == [ix[k - 1] - 1 for k in order]
+    p = g["point_data"]["initialpres"][:, 0]
+    for a, b, c in [(1, 2, 9), (4, 1, 12)]:
+        na, nb, nc = ix[a - 1] - 1, ix[b - 1] - 1, ix[c - 1] - 1
+        assert abs(p[nc] - 0.5 * (p[na] + p[nb])) <= 1e-5 * max(1e-3, abs(p[nc]))

@@ -75,3 +75,37 @@ def test_printnode_layout(golden, tmp_path):
     h = read_history("%s_up_node_1.txt" % prefix)
     r = fx["hist"][0][:4]
     assert np.abs(h[:, 2:] - r[:, 2:]).max() <= 1.5e-10
+
+
+def test_result_vtk_holds_the_state(golden, tmp_path):
+    """pres (write_mesh_res_pm, Write_vtk.f:912-1399): the state and the
+    recovered fields in <prefix>_istep_<n>.vtk, printed with 5 digits."""
+    from poromec_gb300.deck import read_vtk
+    fx = golden("exemplo1_mesh0_t2")
+    path = write_linear_deck(fx, str(tmp_path), "r", nsteps=2)
+    with open(path) as fh:
+        text = fh.read().replace("pnsf\nnext", "pnsf\npres\nnext")
+    with open(path, "w") as fh:
+        fh.write(text)
+    d = Deck(path)
+    prefix = os.path.join(str(tmp_path), "r")
+    m, n = d.run(prefix)
+    assert n == 2
+    g = read_vtk(prefix + "_istep_2.vtk")
+    assert g["field"]["CYCLE"] == [2] and g["field"]["TIME_S"] == [2 * float(fx["dt"])]
+    assert set(g["cell_types"]) == {25} and g["points"].shape[0] == int(fx["nnode"])
+    u, _, dp = m.get_state()
+    tx, txb, txe, fl = m.stress()
+
+    def close(a, b):
+        return np.all(np.abs(a - b) <= 5e-5 * np.abs(b) + 1e-12 * max(1.0, np.abs(b).max()))
+
+    assert close(g["point_data"]["desloc"], u[:, :3])
+    fnno = fx["fnno"] == 1
+    assert close(g["point_data"]["pressao"][fnno, 0], u[fnno, 3])
+    assert close(g["point_data"]["deltaPressao"][fnno, 0], dp[fnno])
+    full = g["point_data"]["totalStress"].reshape(-1, 3, 3)
+    assert close(full[fnno, 0, 0], tx[fnno, 0]) and close(full[fnno, 2, 2], tx[fnno, 2])
+    assert close(full[fnno, 0, 1], tx[fnno, 3]) and close(full[fnno, 1, 2], tx[fnno, 4])
+    assert close(g["point_data"]["darcyFlux"][fnno], fl[fnno])
+    assert close(g["point_data"]["porosity"][fnno, 0], m.get_porosity()[fnno])
