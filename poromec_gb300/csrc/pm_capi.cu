@@ -787,34 +787,40 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   // the PCG form (product fused with p.Ap), as the solver runs it: it writes
   // only ks->pq and ks->alpha, which every solver's init sets again
   PM_CUDA(cudaMemsetAsync(h->D.ks, 0, sizeof(pm::KrylovScalars), s));
-  constexpr int kReps = 5;
-  float best = 0.f;
-  int best_c = 1;
-  for (int c : pm::kCfShapes) {
+  constexpr int kReps = 5, kPasses = 2, kWarm = 10;
+  std::vector<int> cand;
+  for (int c : pm::kCfShapes)
     // the record kernel: only where two records per warp fit in shared
     // memory, and not for batches (it does not skip converged instances)
-    if (c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) continue;
+    if (!(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0))) cand.push_back(c);
+  auto run = [&](int c) {
     const pm::CompVals C = h->P.comp(c);
-    auto run = [&]() {
-      return h->ninst > 0 ? pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s)
-                          : pm::spmvc_pcg(P, C, h->D.kv32.c, h->D.dx, h->D.xs, h->D.ks,
-                                          h->D.partial, h->D.counter, s);
-    };
-    PM_CUDA(run());
-    PM_CUDA(cudaEventRecord(h->ev[0], s));
-    for (int k = 0; k < kReps; ++k) PM_CUDA(run());
-    PM_CUDA(cudaEventRecord(h->ev[1], s));
-    PM_CUDA(cudaEventSynchronize(h->ev[1]));
-    float ms = 0.f;
-    PM_CUDA(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
-    if (h->debug) fprintf(stderr, "spmv autotune: shape %2d  %.4f ms\n", c, ms / kReps);
-    if (c == pm::kCfShapes[0] || ms < best) {
-      best = ms;
-      best_c = c;
+    return h->ninst > 0 ? pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s)
+                        : pm::spmvc_pcg(P, C, h->D.kv32.c, h->D.dx, h->D.xs, h->D.ks,
+                                        h->D.partial, h->D.counter, s);
+  };
+  // clocks settle before the first timing
+  for (int k = 0; k < kWarm; ++k) PM_CUDA(run(cand[0]));
+  h->launches += kWarm;
+  std::vector<float> best_ms(cand.size(), 1e30f);
+  for (int pass = 0; pass < kPasses; ++pass)
+    for (size_t i = 0; i < cand.size(); ++i) {
+      PM_CUDA(run(cand[i]));
+      PM_CUDA(cudaEventRecord(h->ev[0], s));
+      for (int k = 0; k < kReps; ++k) PM_CUDA(run(cand[i]));
+      PM_CUDA(cudaEventRecord(h->ev[1], s));
+      PM_CUDA(cudaEventSynchronize(h->ev[1]));
+      float ms = 0.f;
+      PM_CUDA(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+      best_ms[i] = std::min(best_ms[i], ms / kReps);
+      h->launches += 1 + kReps;
     }
-    h->launches += 1 + kReps;
+  size_t bi = 0;
+  for (size_t i = 0; i < cand.size(); ++i) {
+    if (h->debug) fprintf(stderr, "spmv autotune: shape %3d  %.4f ms\n", cand[i], best_ms[i]);
+    if (best_ms[i] < best_ms[bi]) bi = i;
   }
-  h->shape = best_c;
+  h->shape = cand[bi];
   return PM_OK;
 }
 

@@ -132,10 +132,13 @@ struct CompVals {
   int ca_grid;   // its CTAs (resident on all SMs)
   int shape;  // SpMV shape: 10 * (0: 8, 1: 16, 2: 32 lanes per node) + columns
               // per lane and trip (1, 2, 4), + 100 for packed two-row FP32
-              // arithmetic; kCaShape: the record kernel
+              // arithmetic; 214: shape 14 held to 64 registers (4 CTAs per
+              // SM), 312 / 314: shapes 112 / 114 held to 4 / 3 CTAs per SM;
+              // kCaShape: the record kernel
 };
 constexpr int kCaShape = 90;
-constexpr int kCfShapes[] = {1, 2, 4, 11, 12, 14, 21, 22, 24, 104, 112, 114, 124, kCaShape};
+constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,
+                              104, 112, 114, 124, 214, 312, 314, kCaShape};
 cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
 cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s);
 // Dynamic shared memory of the record kernel for a given record size and

@@ -624,8 +624,8 @@ __device__ __forceinline__ void cf_rows(const float* __restrict__ h,
 // chosen per matrix by the autotuner.  With S = 32 a warp reads each panel
 // row as full 128-byte lines; with S = 8 four nodes share a warp and each
 // load instruction touches four lines.
-template <int MODE, int S, int U, bool PK>
-__global__ void __launch_bounds__(256)
+template <int MODE, int S, int U, bool PK, int MINB>
+__global__ void __launch_bounds__(256, MINB)
     k_spmv_cf(PanelView P, const float* __restrict__ vh, const int8_t* __restrict__ vl,
               const float2* __restrict__ xp, double* __restrict__ y, const double* __restrict__ xd,
               KrylovScalars* ks, double* partial, unsigned* counter) {
@@ -1386,11 +1386,11 @@ int resident_grid(K kernel) {
   return g < kRedBlocks ? g : kRedBlocks;
 }
 
-template <int MODE, int S, int U, bool PK = false>
+template <int MODE, int S, int U, bool PK = false, int MINB = 1>
 void launch_cf(const PanelView& P, CompVals C, const float2* xp, double* y, const double* xd,
                KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s) {
-  static const int grid = resident_grid(k_spmv_cf<MODE, S, U, PK>);
-  k_spmv_cf<MODE, S, U, PK><<<grid, 256, 0, s>>>(
+  static const int grid = resident_grid(k_spmv_cf<MODE, S, U, PK, MINB>);
+  k_spmv_cf<MODE, S, U, PK, MINB><<<grid, 256, 0, s>>>(
       P, C.hi, C.lo, xp, y, xd, ks, partial, counter);
 }
 
@@ -1449,6 +1449,9 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
     case 112: launch_cf<MODE, 16, 2, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 114: launch_cf<MODE, 16, 4, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 124: launch_cf<MODE, 32, 4, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 214: launch_cf<MODE, 16, 4, false, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 314: launch_cf<MODE, 16, 4, true, 3>(P, C, xp, y, xd, ks, partial, counter, s); break;
+    case 312: launch_cf<MODE, 16, 2, true, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
     default: launch_cf<MODE, 8, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
   }
 }
