@@ -444,6 +444,8 @@ int gmres_run(Handle* h, const double* d_b, double* x, double tol, int maxit, in
   return PM_E_NOCONV;
 }
 
+int check_cs_fault(Handle* h);
+
 // One Krylov solve of K x = b on the device (solv_pm, Solv.f:27-780).
 //
 // comp = false: the reference's FP64 iteration on the FP64 panels.
@@ -651,6 +653,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     h->err = "solver must be 1 (pcg), 2 (gmres), 7 (minres) or 11 (rpsqmr)";
     return PM_E_ARG;
   }
+  if (comp && h->shape == pm::kCsShape) PM_TRY(check_cs_fault(h));
   PM_CUDA(cudaEventRecord(e1, h->stream));
   // x.Kx of the solver log (one more product with the converged x)
   const double* xs = (comp && solver == 1) ? d_x : V.x;
@@ -772,12 +775,26 @@ int solve_mixed(Handle* h, int solver, const double* d_b, double* d_x, double to
 // after one warm-up, with CUDA events on the launching stream, and keeps the
 // fastest for the handle's lifetime (graphs captured later bake it in).
 // PM_SPMV_SHAPE=<code> in the environment fixes the choice instead.
+// The streamed SpMV's fault flag (a bounded pipeline wait gave up): cleared
+// and reported once.
+int check_cs_fault(Handle* h) {
+  if (!h->P.fault) return PM_OK;
+  int f = 0;
+  PM_CUDA(cudaMemcpyAsync(&f, h->P.fault, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  PM_CUDA(cudaStreamSynchronize(h->stream));
+  if (!f) return PM_OK;
+  PM_CUDA(cudaMemsetAsync(h->P.fault, 0, sizeof(int), h->stream));
+  h->err = "streamed SpMV: a pipeline wait gave up (results of that product are invalid)";
+  return PM_E_CUDA;
+}
+
 int tune_spmvc(Handle* h, cudaStream_t s) {
   if (h->shape) return PM_OK;
   if (const char* env = std::getenv("PM_SPMV_SHAPE")) {
     const int u = std::atoi(env);
     for (int c : pm::kCfShapes)
-      if (u == c && !(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0))) {
+      if (u == c && !(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) &&
+          !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0))) {
         h->shape = u;
         return PM_OK;
       }
@@ -792,7 +809,9 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
   for (int c : pm::kCfShapes)
     // the record kernel: only where two records per warp fit in shared
     // memory, and not for batches (it does not skip converged instances)
-    if (!(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0))) cand.push_back(c);
+    if (!(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) &&
+        !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0)))
+      cand.push_back(c);
   auto run = [&](int c) {
     const pm::CompVals C = h->P.comp(c);
     return h->ninst > 0 ? pm::spmvc(P, C, h->D.kv32.c, h->D.dx, s)
@@ -815,6 +834,10 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
       best_ms[i] = std::min(best_ms[i], ms / kReps);
       h->launches += 1 + kReps;
     }
+  // a shape whose pipeline reported a fault is not chosen
+  if (check_cs_fault(h) != PM_OK)
+    for (size_t i = 0; i < cand.size(); ++i)
+      if (cand[i] == pm::kCsShape) best_ms[i] = 1e30f;
   size_t bi = 0;
   for (size_t i = 0; i < cand.size(); ++i) {
     if (h->debug) fprintf(stderr, "spmv autotune: shape %3d  %.4f ms\n", cand[i], best_ms[i]);
@@ -838,7 +861,7 @@ int ensure_comp(Handle* h, cudaStream_t s) {
     h->launches += 1;
     PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
   }
-  if (h->P.rec && (h->shape == 0 || h->shape == pm::kCaShape)) {
+  if (h->P.rec && (h->shape == 0 || h->shape == pm::kCaShape || h->shape == pm::kCsShape)) {
     h->launches += 1;
     PM_CUDA(pm::split_records(h->P.view(), h->P.val, h->P.comp(h->shape), s));
   }
@@ -1157,7 +1180,8 @@ void free_all(Handle* h) {
                   D.kv.v, D.kv.v0, D.kv.w0, D.kv.w00, D.kv.z0, D.ks, D.partial, D.counter,
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
                   P.val32, P.valh, P.vall, P.rec, P.rec_off, P.node_val_off, P.node_W,
-                  P.order};
+                  P.order, P.cs_desc, P.cs_batch_slot, P.cs_batch_off, P.cs_batch_bytes,
+                  P.cs_cta_batch, P.fault};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})
@@ -1721,6 +1745,7 @@ int pm_spmv(pm_handle hh, const double* x, double* y) {
   PM_TRY(spmv_op(h, h->D.bx, h->D.by, h->stream));
   PM_CUDA(cudaMemcpyAsync(y, h->D.by, sizeof(double) * h->neq, cudaMemcpyDeviceToHost, h->stream));
   PM_CUDA(cudaStreamSynchronize(h->stream));
+  if (h->precision == PM_FP32C_REFINE && h->shape == pm::kCsShape) PM_TRY(check_cs_fault(h));
   return PM_OK;
 }
 

@@ -52,6 +52,11 @@ struct Panels {
   uint8_t* rec = nullptr;
   int64_t* rec_off = nullptr;
   int rec_max = 0, ca_warps = 0, ca_grid = 0;
+  int4* cs_desc = nullptr;
+  int32_t *cs_batch_slot = nullptr, *cs_batch_bytes = nullptr, *cs_cta_batch = nullptr;
+  int64_t* cs_batch_off = nullptr;
+  int cs_grid = 0, cs_nstage = 0, cs_stage_bytes = 0;
+  int* fault = nullptr;
   // batches: instance of each active node, done flag of each instance
   int32_t* node_inst = nullptr;
   int* inst_done = nullptr;
@@ -66,7 +71,10 @@ struct Panels {
     return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols, node_inst, inst_done};
   }
   CompVals comp(int shape) const {
-    return CompVals{valh, vall, rec, rec_off, rec_max, ca_warps, ca_grid, shape};
+    return CompVals{valh,          vall,          rec,          rec_off,        rec_max,
+                    ca_warps,      ca_grid,       cs_desc,      cs_batch_slot,  cs_batch_off,
+                    cs_batch_bytes, cs_cta_batch, cs_grid,      cs_nstage,      cs_stage_bytes,
+                    fault,         shape};
   }
 };
 

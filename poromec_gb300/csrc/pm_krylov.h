@@ -130,21 +130,40 @@ struct CompVals {
   int rec_max;   // bytes of the largest record
   int ca_warps;  // warps per CTA of the record kernel (two records each in smem)
   int ca_grid;   // its CTAs (resident on all SMs)
+  // Streamed record kernel (shape kCsShape): the records cut into batches of
+  // up to kCsNodes consecutive nodes (one contiguous byte range each), runs
+  // of batches per CTA, and per visiting slot (eq0, d, W, byte offset of the
+  // node's record in its batch).
+  const int4* cs_desc;
+  const int32_t* cs_batch_slot;   // first slot of each batch (+ end)
+  const int64_t* cs_batch_off;    // byte offset of each batch in rec
+  const int32_t* cs_batch_bytes;  // bytes of each batch
+  const int32_t* cs_cta_batch;    // first batch of each CTA (+ end)
+  int cs_grid, cs_nstage, cs_stage_bytes;
+  int* fault;  // set when a pipeline wait of the streamed kernel gave up
   int shape;  // SpMV shape: 10 * (0: 8, 1: 16, 2: 32 lanes per node) + columns
               // per lane and trip (1, 2, 4), + 100 for packed two-row FP32
               // arithmetic; 214: shape 14 held to 64 registers (4 CTAs per
               // SM), 312 / 314: shapes 112 / 114 held to 4 / 3 CTAs per SM;
-              // kCaShape: the record kernel
+              // kCaShape: the record kernel; kCsShape: the streamed record
+              // kernel
 };
-constexpr int kCaShape = 90;
+constexpr int kCaShape = 90, kCsShape = 91;
+constexpr int kCsWarps = 8;                // consumer warps of the streamed kernel
+constexpr int kCsNodes = 2 * kCsWarps;     // nodes per batch (one per half-warp)
+constexpr int kCsMaxStages = 4;
 constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,
-                              104, 112, 114, 124, 214, 312, 314, kCaShape};
+                              104, 112, 114, 124, 214, 312, 314, kCaShape, kCsShape};
 cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
 cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s);
 // Dynamic shared memory of the record kernel for a given record size and
 // warp count, and the set-up of its launch attributes (once per process).
 int ca_smem_bytes(int rec_max, int warps);
 cudaError_t ca_configure(int rec_max, int* warps, int* grid);
+// Shared memory of the streamed kernel for nstage stages of stage_bytes, and
+// the stage count that fits (0: the kernel is not available for this mesh).
+int cs_smem_bytes(int nstage, int stage_bytes);
+cudaError_t cs_configure(int stage_bytes, int* nstage, int* ctas);
 cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s);
 cudaError_t spmvc(const PanelView& P, CompVals C, const float2* xp, double* y, cudaStream_t s);
 // the PCG form of the compensated product: y = A x and ks->alpha = ks->d / (y . xd)

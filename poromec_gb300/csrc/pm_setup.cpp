@@ -1,6 +1,8 @@
 // pm_setup.cpp -- host set-up of the 'mesh' macro (Main.f:481-870):
 // equation numbering, node graph, node-panel matrix structure, element
 // colouring and the element -> panel slot map, then upload to the device.
+#include <cstdio>
+#include <cstdlib>
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -311,6 +313,75 @@ int build_rec_layout(Handle* h) {
   if (ca_configure(rmax, &P.ca_warps, &P.ca_grid) != cudaSuccess) {
     h->err = "record SpMV set-up failed";
     return PM_E_CUDA;
+  }
+  // streamed record kernel: batches of up to kCsNodes consecutive records
+  // (one warp per node), a stage holds the largest batch
+  const int stage_bytes = kCsNodes * rmax;
+  int nstage = 0, ctas = 0, sms = 0, dev = 0;
+  if (cs_configure(stage_bytes, &nstage, &ctas) != cudaSuccess ||
+      cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    h->err = "streamed SpMV set-up failed";
+    return PM_E_CUDA;
+  }
+  sms *= ctas;
+  if (nstage >= 2 && nact > 0) {
+    std::vector<int4> desc(nact);
+    std::vector<int32_t> bslot, bbytes;
+    std::vector<int64_t> boff;
+    int64_t total = 0;
+    for (int i = 0; i < nact;) {
+      const int k0 = h->h_order[i];
+      const int64_t start = off[k0];
+      int j = i, bytes = 0;
+      while (j < nact && j - i < kCsNodes) {
+        const int k = h->h_order[j];
+        const int Wp = (h->h_W[k] + 3) & ~3;
+        const int R = 4 * h->h_d[k] * Wp + ((h->h_d[k] * Wp + 15) & ~15) + 4 * Wp;
+        desc[j] = make_int4(h->h_eq0[k], h->h_d[k], h->h_W[k], (int)(off[k] - start));
+        bytes += R;
+        ++j;
+      }
+      bslot.push_back(i);
+      boff.push_back(start);
+      bbytes.push_back(bytes);
+      total += bytes;
+      i = j;
+    }
+    const int nb = (int)bslot.size();
+    bslot.push_back(nact);
+    // runs of batches per CTA, balanced by estimated time: a batch costs its
+    // bytes at the CTA's share of HBM plus a fixed part (the gather latency
+    // and the stage hand-over, about the time of 24 KB), so that CTAs with
+    // many small boundary-node batches do not set the kernel's duration
+    const int64_t kFixed = 24 * 1024;
+    int64_t cost_total = total + kFixed * (int64_t)nb;
+    const int grid = std::max(1, std::min(sms, nb));
+    std::vector<int32_t> cta(grid + 1, nb);
+    cta[0] = 0;
+    int64_t acc = 0;
+    int c = 1;
+    for (int b = 0; b < nb && c < grid; ++b) {
+      acc += bbytes[b] + kFixed;
+      while (c < grid && acc * grid >= cost_total * c) cta[c++] = b + 1;
+    }
+    for (; c < grid; ++c) cta[c] = nb;
+    if ((st = upload(h, &P.cs_desc, desc.data(), desc.size()))) return st;
+    if ((st = upload(h, &P.cs_batch_slot, bslot.data(), bslot.size()))) return st;
+    if ((st = upload(h, &P.cs_batch_off, boff.data(), boff.size()))) return st;
+    if ((st = upload(h, &P.cs_batch_bytes, bbytes.data(), bbytes.size()))) return st;
+    if ((st = upload(h, &P.cs_cta_batch, cta.data(), cta.size()))) return st;
+    if ((st = upload<int>(h, &P.fault, nullptr, 1))) return st;
+    if (cudaMemset(P.fault, 0, sizeof(int)) != cudaSuccess) {
+      h->err = "cudaMemset failed";
+      return PM_E_CUDA;
+    }
+    P.cs_grid = grid;
+    P.cs_nstage = nstage;
+    P.cs_stage_bytes = stage_bytes;
+    if (getenv("PM_DEBUG"))
+      fprintf(stderr, "streamed SpMV: %d batches, %d CTAs (%d per SM), %d stages of %d bytes\n",
+              nb, grid, ctas, nstage, stage_bytes);
   }
   return PM_OK;
 }

@@ -14,6 +14,7 @@
 // convergence without changing the result.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/poromec_gb300.h"
@@ -862,6 +863,247 @@ __global__ void __launch_bounds__(512, 1)
   }
 }
 
+// ---- streamed record kernel: batches of node records moved by TMA ---------
+// The records of the visiting order are cut on the host into batches of up
+// to kCsNodes consecutive nodes, each one contiguous 16-byte aligned byte
+// range, and each CTA owns a run of batches balanced by estimated time.  The
+// batches stream through C.cs_nstage shared-memory stages: a producer warp
+// issues one cp.async.bulk per batch, completing on the stage's mbarrier, and
+// each half-warp of the kCsWarps consumer warps computes one node of the
+// batch from shared memory.  The bytes in flight per SM are the stages ahead,
+// independent of the registers.  Every mbarrier wait is bounded: a warp whose
+// wait gives up sets *C.fault, the producer then waits with the same bound
+// for its copies in flight, and every thread still takes part in the grid
+// reduction, so the reduction counter stays consistent.
+//
+// Measured on the 56^3 cube (2.35 M equations) it takes 1.04 ms against
+// 0.63 ms for the register kernels: shared memory holds two stages of 16
+// whole node records (104 KB each), i.e. 16 node streams per SM, while the
+// register kernels keep 48 streams of 4-column chunks in the larger register
+// file; the gather latency of the x pairs is then what the streamed kernel
+// cannot hide.  It stays an autotuner candidate.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// a non-blocking poll with a short sleep, given up after 2^30 clock cycles
+// (about half a second; a batch lands in microseconds)
+constexpr long long kCsWaitCycles = 1ll << 30;
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  if (mbar_test(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (clock64() - t0 < kCsWaitCycles) {
+    if (mbar_test(bar, parity)) return true;
+    __nanosleep(32);
+  }
+  return mbar_test(bar, parity);
+}
+
+// Rows of one node from its record in shared memory by a 16-lane half-warp:
+// lane t takes column quads t, t + 16, ... ; the 4 x-pair gathers of the next
+// quad are issued before the products of the current one.
+template <int D>
+__device__ __forceinline__ void cs_rows(const float4* __restrict__ h4,
+                                        const unsigned* __restrict__ q4,
+                                        const int4* __restrict__ c4,
+                                        const float2* __restrict__ xp, int nq, int t,
+                                        F2 (&a)[4]) {
+  float2 xn[4];
+  int j = t;
+  if (j < nq) {
+    const int4 cc = c4[j];
+    xn[0] = xp[cc.x];
+    xn[1] = xp[cc.y];
+    xn[2] = xp[cc.z];
+    xn[3] = xp[cc.w];
+  }
+  for (; j < nq; j += 16) {
+    const float2 x0 = xn[0], x1 = xn[1], x2 = xn[2], x3 = xn[3];
+    const int jn = j + 16;
+    if (jn < nq) {
+      const int4 cc = c4[jn];
+      xn[0] = xp[cc.x];
+      xn[1] = xp[cc.y];
+      xn[2] = xp[cc.z];
+      xn[3] = xp[cc.w];
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      const float4 hv = h4[r * nq + j];
+      const unsigned qv = q4[r * nq + j];
+      f2_fma_s(a[r], hv.x, qb_scale(qv, 0), x0.x, x0.y);
+      f2_fma_s(a[r], hv.y, qb_scale(qv, 1), x1.x, x1.y);
+      f2_fma_s(a[r], hv.z, qb_scale(qv, 2), x2.x, x2.y);
+      f2_fma_s(a[r], hv.w, qb_scale(qv, 3), x3.x, x3.y);
+    }
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// kCsNodes consumer warps (one node of each batch each) and one producer
+// warp, whose lane 0 issues the copies.  Per stage two mbarriers: full (the
+// batch landed: one arrival with the byte count, completed by the copy) and
+// empty (the kCsNodes consumer warps are done with it).  The warps never
+// wait for each other, only for their data, so the gather latency of one
+// warp overlaps the arithmetic of the others.
+template <int MODE>
+__global__ void __launch_bounds__((kCsWarps + 1) * 32)
+    k_spmv_cs(PanelView P, CompVals C, const float2* __restrict__ xp, double* __restrict__ y,
+              const double* __restrict__ xd, KrylovScalars* ks, double* partial,
+              unsigned* counter) {
+  if (MODE != 0)
+    if (krylov_skip(ks, true)) return;
+  extern __shared__ __align__(128) unsigned char cs_smem[];
+  unsigned long long* full = reinterpret_cast<unsigned long long*>(cs_smem);
+  unsigned long long* empty = full + kCsMaxStages;
+  const int nst = C.cs_nstage, sbytes = C.cs_stage_bytes;
+  unsigned char* stages = cs_smem + 128;
+  const int lane = threadIdx.x & 31, w = (int)(threadIdx.x >> 5);
+  const int half = lane >> 4, t = lane & 15;
+  const bool producer = w == kCsWarps;
+  float2* o_sc = reinterpret_cast<float2*>(stages + (size_t)nst * sbytes) + w * 32;
+  int* o_eq = reinterpret_cast<int*>(stages + (size_t)nst * sbytes +
+                                     (size_t)(kCsWarps + 1) * 32 * sizeof(float2)) + w * 32;
+  const int b0 = C.cs_cta_batch[blockIdx.x], b1 = C.cs_cta_batch[blockIdx.x + 1];
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < nst; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], kCsWarps);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  double dsum = 0.0;
+  int count = 0;  // staged rows of this warp (warp-uniform)
+  auto flush = [&]() {
+    __syncwarp();
+    if (lane < count) {
+      const float2 sc = o_sc[lane];
+      const int e = o_eq[lane];
+      const double v = double(sc.x) + double(sc.y);
+      y[e] = v;
+      if (MODE != 0) dsum += v * xd[e];
+    }
+    __syncwarp();
+    count = 0;
+  };
+  if (producer) {
+    if (lane == 0) {
+      int j = b0;
+      bool ok = true;
+      for (; j < b1 && ok; ++j) {
+        const int k = (j - b0) % nst, use = (j - b0) / nst;
+        // the consumers' release of the batch that used this stage before
+        if (use > 0) ok = mbar_wait_bounded(&empty[k], (unsigned)((use - 1) & 1));
+        if (!ok) break;
+        fence_proxy_async();
+        const unsigned bytes = (unsigned)C.cs_batch_bytes[j];
+        mbar_expect_tx(&full[k], bytes);
+        bulk_g2s(stages + (size_t)k * sbytes, C.rec + C.cs_batch_off[j], bytes, &full[k]);
+      }
+      if (!ok) {
+        atomicExch(C.fault, 1);
+        // the copies issued and maybe not consumed land before the CTA leaves
+        for (int i = std::max(b0, j - nst); i < j; ++i)
+          mbar_wait_bounded(&full[(i - b0) % nst], (unsigned)(((i - b0) / nst) & 1));
+      }
+    }
+  } else {
+    for (int j = b0; j < b1; ++j) {
+      const int k = (j - b0) % nst;
+      const int s0 = C.cs_batch_slot[j], s1 = C.cs_batch_slot[j + 1];
+      const int slot = s0 + 2 * w + half;
+      const bool has = slot < s1;
+      const int4 dd = has ? C.cs_desc[slot] : make_int4(0, 0, 0, 0);
+      const bool ok = mbar_wait_bounded(&full[k], (unsigned)(((j - b0) / nst) & 1));
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) atomicExch(C.fault, 1);
+        break;
+      }
+      const int d = dd.y;
+      F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      if (has) {
+        const int Wp = (dd.z + 3) & ~3, nq = Wp >> 2;
+        const unsigned char* b = stages + (size_t)k * sbytes + dd.w;
+        const float4* h4 = reinterpret_cast<const float4*>(b);
+        const unsigned* q4 = reinterpret_cast<const unsigned*>(b + 4 * d * Wp);
+        const int4* c4 = reinterpret_cast<const int4*>(b + 4 * d * Wp + ((d * Wp + 15) & ~15));
+        if (d == 4) cs_rows<4>(h4, q4, c4, xp, nq, t, a);
+        else if (d == 3) cs_rows<3>(h4, q4, c4, xp, nq, t, a);
+        else if (d == 2) cs_rows<2>(h4, q4, c4, xp, nq, t, a);
+        else cs_rows<1>(h4, q4, c4, xp, nq, t, a);
+      }
+      __syncwarp();  // this warp has read stage k
+      if (lane == 0) mbar_arrive(&empty[k]);
+      // transposed butterfly within each half-warp (as k_spmv_cf with S = 16)
+      const bool h1 = (t & 8) != 0, h2 = (t & 4) != 0;
+      F2 k0 = h1 ? a[2] : a[0], k1 = h1 ? a[3] : a[1];
+      k0 = f2_add(k0, f2_shfl(h1 ? a[0] : a[2], 8));
+      k1 = f2_add(k1, f2_shfl(h1 ? a[1] : a[3], 8));
+      F2 kk = h2 ? k1 : k0;
+      kk = f2_add(kk, f2_shfl(h2 ? k0 : k1, 4));
+      kk = f2_add(kk, f2_shfl(kk, 2));
+      kk = f2_add(kk, f2_shfl(kk, 1));
+      const int r = (h1 ? 2 : 0) + (h2 ? 1 : 0);
+      // rows of both halves: half 0's d0 rows, then half 1's
+      const int d0 = __shfl_sync(0xffffffffu, d, 0), d1 = __shfl_sync(0xffffffffu, d, 16);
+      if (count + d0 + d1 > 32) flush();
+      if ((t & 3) == 0 && r < d) {
+        o_sc[count + (half ? d0 : 0) + r] = make_float2(kk.s, kk.c);
+        o_eq[count + (half ? d0 : 0) + r] = dd.x + r;
+      }
+      count += d0 + d1;
+    }
+    flush();
+  }
+  if (MODE != 0) {
+    double in[1] = {dsum}, tot[1];
+    if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+      if (MODE == 1) {
+        ks->pq = tot[0];
+        ks->alpha = ks->d / tot[0];
+      } else {
+        ks->alpha = fabs(tot[0]) * (1.0 / (ks->beta * ks->beta));
+      }
+    }
+  }
+}
+
 // FP64 panel values (rows of W) -> node records (layout in CompVals): one
 // warp per node, coalesced on both sides.  hi = fl32(v), qb = 128 +
 // round((v - hi) / hi * 2^31) clamped to [1, 255]; pad columns get hi = 0,
@@ -1394,6 +1636,79 @@ void launch_cf(const PanelView& P, CompVals C, const float2* xp, double* y, cons
       P, C.hi, C.lo, xp, y, xd, ks, partial, counter);
 }
 
+int cs_smem_bytes(int nstage, int stage_bytes) {
+  return 128 + nstage * stage_bytes + (kCsWarps + 1) * 32 * (int)(sizeof(float2) + sizeof(int));
+}
+
+// Stages of the streamed kernel and CTAs per SM (*ctas); fewer than 2
+// stages leaves the kernel out.  The
+// launch attribute is the whole opt-in size less the static shared memory,
+// so that meshes with different stage sizes can share the kernel.
+cudaError_t cs_configure(int stage_bytes, int* nstage, int* ctas) {
+  int dev = 0, optin = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (e != cudaSuccess) return e;
+  // the dynamic part is what is left after the static shared memory of the
+  // kernel variants (the reduction scratch) and the per-CTA reservation
+  int stat = 0;
+  for (const void* k : {(const void*)k_spmv_cs<0>, (const void*)k_spmv_cs<1>,
+                        (const void*)k_spmv_cs<2>}) {
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k)) != cudaSuccess) return e;
+    stat = std::max(stat, (int)fa.sharedSizeBytes);
+  }
+  const int dyn = optin - stat;
+  const int reserve = 1024;
+  *nstage = 0;
+  *ctas = 0;
+  // one CTA per SM with as many stages as fit (a deeper pipeline); two CTAs
+  // of two stages where one CTA holds fewer than three
+  int n = kCsMaxStages;
+  while (n > 0 && cs_smem_bytes(n, stage_bytes) > dyn) --n;
+  if (n >= 3) {
+    *nstage = n;
+    *ctas = 1;
+  } else if (2 * (cs_smem_bytes(2, stage_bytes) + stat + reserve) <= per_sm) {
+    *nstage = 2;
+    *ctas = 2;
+  } else if (n == 2) {
+    *nstage = 2;
+    *ctas = 1;
+  }
+  if (*nstage == 0) return cudaSuccess;
+  static std::once_flag once;
+  static cudaError_t ae = cudaSuccess;
+  std::call_once(once, [&]() {
+    for (const void* k : {(const void*)k_spmv_cs<0>, (const void*)k_spmv_cs<1>,
+                          (const void*)k_spmv_cs<2>}) {
+      if (ae == cudaSuccess)
+        ae = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+      if (ae == cudaSuccess)
+        ae = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared);
+    }
+  });
+  if (ae != cudaSuccess) return ae;
+  // two CTAs only if they are resident together
+  if (*ctas == 2) {
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_spmv_cs<1>, (kCsWarps + 1) * 32,
+                                                      cs_smem_bytes(2, stage_bytes));
+    if (e != cudaSuccess) return e;
+    if (nb < 2) {
+      int n = kCsMaxStages;
+      while (n > 0 && cs_smem_bytes(n, stage_bytes) > dyn) --n;
+      *nstage = n >= 2 ? n : 0;
+      *ctas = n >= 2 ? 1 : 0;
+    }
+  }
+  return cudaSuccess;
+}
+
 int ca_smem_bytes(int rec_max, int warps) {
   return warps * (2 * rec_max + 32 * (int)(sizeof(float2) + sizeof(int)));
 }
@@ -1436,6 +1751,11 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
     case kCaShape:
       k_spmv_ca<MODE><<<C.ca_grid, C.ca_warps * 32, ca_smem_bytes(C.rec_max, C.ca_warps), s>>>(
           P, C, xp, y, xd, ks, partial, counter);
+      break;
+    case kCsShape:
+      k_spmv_cs<MODE><<<C.cs_grid, (kCsWarps + 1) * 32,
+                        cs_smem_bytes(C.cs_nstage, C.cs_stage_bytes), s>>>(P, C, xp, y, xd, ks,
+                                                                           partial, counter);
       break;
     case 2: launch_cf<MODE, 8, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 4: launch_cf<MODE, 8, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
