@@ -961,6 +961,14 @@ std::string fortran_e(double v, int w, int dd, int edig) {
   return b;
 }
 
+// Fortran Dw.d: as Ew.d with the exponent letter D
+std::string fortran_d(double v, int w, int dd) {
+  std::string r = fortran_e(v, w, dd, 2);
+  const size_t k = r.find('E');
+  if (k != std::string::npos) r[k] = 'D';
+  return r;
+}
+
 void vtk_head(FILE* f, const char* title, bool time, double t, int istep) {
   std::fprintf(f, "# vtk DataFile Version 3.0\n%-30s\nASCII\nDATASET UNSTRUCTURED_GRID\n",
                title);
@@ -1269,6 +1277,7 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
     int left;
   };
   std::vector<Frame> loops;
+  bool log_open = false;
   int st = PM_OK;
   for (size_t pc = 0; pc < d->prog.size(); ++pc) {
     const Op& op = d->prog[pc];
@@ -1302,6 +1311,23 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
           return st;
         istep += 1;
         t = t + s.dt;
+        // the solver log (Iters.f 'flog' lines; the layout of the shipped
+        // golden logs): iterations, energy norm x.Kx, tolerance, seconds
+        double tm[8] = {0};
+        pm_get_timers(h, tm, 8);
+        const std::string ln = std::string(prefix) + "_log_1.txt";
+        FILE* lf = std::fopen(ln.c_str(), log_open ? "a" : "w");
+        if (!lf) return PM_E_ARG;
+        if (!log_open) std::fputs("Solver control flop.\n", lf);
+        log_open = true;
+        static const char* names[] = {"", "PCG:", "GMRES2:", "", "", "", "", "MINRES:", "", "",
+                                      "", "RPSQMR:"};
+        const char* nm = s.solver >= 0 && s.solver < 12 && names[s.solver][0] ? names[s.solver]
+                                                                               : "SOLVER:";
+        std::fprintf(lf, "%s  it %9d energy norm %s tol %s time %20.2f\n", nm, info.iters,
+                     fortran_d(info.xkx, 20, 10).c_str(), fortran_d(s.solvtol, 20, 10).c_str(),
+                     tm[3] * 1e-3);
+        std::fclose(lf);
         break;
       }
       case OP_PNUP:

@@ -195,13 +195,15 @@ def read_history(path):
 
 
 def read_log(path):
-    its = []
+    """Iteration counts and energy norms (x.Kx) of the solver log's PCG lines."""
+    its, xkx = [], []
     with open(path) as fh:
         for line in fh:
-            m = re.match(r"\s*PCG:\s+it\s+(\d+)", line)
+            m = re.match(r"\s*PCG:\s+it\s+(\d+)\s+energy norm\s+(\S+)", line)
             if m:
                 its.append(int(m.group(1)))
-    return np.array(its, np.int32)
+                xkx.append(float(m.group(2).replace("D", "E")))
+    return np.array(its, np.int32), np.array(xkx)
 
 
 def read_counts(path):
@@ -273,7 +275,7 @@ def convert(ref_root, kind, deck, prefix):
         for k, v in g["cell_data"].items():
             vtk["vtkc_" + k] = v
     counts = read_counts(os.path.join(ddir, prefix + "_t_1.txt"))
-    its = read_log(os.path.join(ddir, prefix + "_log_1.txt"))
+    its, xkx = read_log(os.path.join(ddir, prefix + "_log_1.txt"))
     tol = d["solver_tol"] if d["solver_tol"] != 0.0 else 2.0 ** -53  # smachn
     hnodes = np.array(sorted(hist), np.int32)
     out = dict(nnode=nnode, nnodev=d["nnodev"], numel=numel, nen=nen, nenv=nenv,
@@ -282,7 +284,7 @@ def convert(ref_root, kind, deck, prefix):
                nsteps=d["nsteps"], maxnlit=d["maxnlit"], solver_tol=tol,
                maxit=d["maxit"], reord=int(d["reord"]), hist_nodes=hnodes,
                hist=np.stack([hist[n] for n in hnodes]) if len(hnodes) else np.zeros(0),
-               pcg_iters=its, neq_ref=counts.get("neq", -1), nad_ref=counts.get("nad", -1),
+               pcg_iters=its, pcg_xkx=xkx, neq_ref=counts.get("neq", -1), nad_ref=counts.get("nad", -1),
                nnode_ref=counts.get("nnode", -1), complete=int(not MISSING), **extra, **vtk)
     name = os.path.join(HERE, prefix + ".npz")
     np.savez_compressed(name, **out)

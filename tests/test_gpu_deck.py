@@ -54,6 +54,19 @@ def test_deck_run_matches_golden_histories(golden, tmp_path, name, keys):
             assert np.abs(h[:, 1] - r[:, 1]).max() <= 1e-6                # t, 6 decimals
             assert np.abs(h[:, 2:] - r[:, 2:]).max() <= 1.5e-10, (k, n)
         assert os.path.exists("%s_poro_node_%d.txt" % (prefix, n))
+    # the solver log against the reference's: one PCG line per step; counts
+    # follow rounding on this indefinite system (the mean within 10 %, as the
+    # oracle's); energy norms x.Kx within 1e-8 relative (printed to 10 digits)
+    with open(prefix + "_log_1.txt") as fh:
+        lines = fh.read().splitlines()
+    assert lines[0] == "Solver control flop." and len(lines) == 601
+    its = np.array([int(ln.split()[2]) for ln in lines[1:]])
+    xkx = np.array([float(ln.split()[5].replace("D", "E")) for ln in lines[1:]])
+    ref = fx["pcg_iters"][:600]
+    assert its[0] == ref[0] or abs(its[0] - ref[0]) <= 2
+    assert abs(its.mean() - ref.mean()) <= 0.1 * ref.mean()
+    assert lines[1].startswith("PCG:  it ")
+    assert np.all(np.abs(xkx - fx["pcg_xkx"]) <= 1e-8 * np.abs(fx["pcg_xkx"]) + 1e-13)
 
 
 def test_printnode_layout(golden, tmp_path):

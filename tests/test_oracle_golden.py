@@ -62,6 +62,18 @@ def test_node_histories(golden, name, nsteps, tol):
     assert abs(np.mean(iters) - np.mean(ref_its)) <= 0.1 * np.mean(ref_its)
 
 
+@pytest.mark.parametrize("name", ["exemplo1_mesh0_t2", "exemplo1_mesh0_t2_tetra"])
+def test_energy_norms_of_the_solver_log(golden, name):
+    """x.Kx of every step's solve against the reference's solver log (the
+    'energy norm' of its PCG lines, 10 significant digits)."""
+    fx = golden(name)
+    o = oracle.from_fixture(fx)
+    xkx = np.array([o.step(maxnlit=2, stop_crit=1, solvtol=float(fx["solver_tol"]),
+                           maxit=int(fx["maxit"])).xkx for _ in range(600)])
+    ref = fx["pcg_xkx"]
+    assert np.all(np.abs(xkx - ref) <= 1e-9 * np.abs(ref) + 1e-13)
+
+
 def test_first_step_known_answers(golden):
     fx = golden("exemplo1_mesh0_t2")
     o = oracle.from_fixture(fx)
