@@ -301,7 +301,8 @@ int pm_deck_create(pm_deck d, pm_handle* h);
  * files of pm_deck_write_geo / pm_deck_write_res (pres with every field), and
  * the solver log <prefix>_log_1.txt (one line per solv: iterations, energy
  * norm x.Kx and tolerance in D20.10, seconds; the layout of the shipped golden
- * logs).  format 0 writes printnode's
+ * logs) and, at the end, <prefix>_t_1.txt (phase seconds ELMT / TFORM / SOLVR /
+ * TOTAL and the sizes neq, nad, nnode, numel, colors, as write_log_file).  format 0 writes printnode's
  * (i9,10e18.10) rows; format 1 the column layout of the golden runs shipped
  * with the reference (i9, f30.6, f30.10 ...).  *nsteps = steps run. */
 int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nsteps);

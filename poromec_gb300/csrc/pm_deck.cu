@@ -20,6 +20,7 @@
 // loop (their runs accept the second nonlinear iteration, i.e. stop_crit 1),
 // and loads of types 39-43 given inline as "type ncomp v1 .. vncomp" (a
 // one-row table whose first column is the time) instead of a file name.
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1279,6 +1280,8 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
   std::vector<Frame> loops;
   bool log_open = false;
   int st = PM_OK;
+  double phase_s[4] = {0, 0, 0, 0}, tform_s = 0.0;  // ELMT parts, SOLVR; TFORM
+  const auto wall0 = std::chrono::steady_clock::now();
   for (size_t pc = 0; pc < d->prog.size(); ++pc) {
     const Op& op = d->prog[pc];
     switch (op.kind) {
@@ -1315,6 +1318,7 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
         // golden logs): iterations, energy norm x.Kx, tolerance, seconds
         double tm[8] = {0};
         pm_get_timers(h, tm, 8);
+        for (int q = 0; q < 4; ++q) phase_s[q] += tm[q] * 1e-3;
         const std::string ln = std::string(prefix) + "_log_1.txt";
         FILE* lf = std::fopen(ln.c_str(), log_open ? "a" : "w");
         if (!lf) return PM_E_ARG;
@@ -1339,10 +1343,12 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
             return st;
         break;
       case OP_PNSF: {
+        const auto ts0 = std::chrono::steady_clock::now();
         if ((st = pm_stress(h, tx.data(), txb.data(), txe.data(), fl.data())) != PM_OK ||
             (st = pm_get_state(h, u.data(), nullptr, nullptr)) != PM_OK ||
             (st = pm_get_porosity(h, poro.data())) != PM_OK)
           return st;
+        tform_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - ts0).count();
         if (d->fstress0) {
           // pnsf adds the initial stress (Main.f:2360-2370), then effective_stress
           for (size_t q = 0; q < tx.size(); ++q) {
@@ -1383,6 +1389,28 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
     }
   }
   if (nsteps) *nsteps = istep;
+  // the run's log (write_log_file, Write_log.f:46-408): phase times in
+  // seconds, then the sizes of the mesh and of the linear system
+  int neq = 0, nc = 0;
+  int64_t nad = 0, nnz = 0;
+  if ((st = pm_get_sizes(h, &neq, &nad, &nc, &nnz)) != PM_OK) return st;
+  const double wall =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
+  const std::string tn = std::string(prefix) + "_t_1.txt";
+  FILE* tf = std::fopen(tn.c_str(), "w");
+  if (!tf) return PM_E_ARG;
+  std::fprintf(tf, "# Arquivo de log do poro mecanico\nTempos (seg):\n"
+                   "Resolucao do tempo:  1.00E-06\n");
+  const std::pair<const char*, double> rows[] = {
+      {"ELMT", phase_s[0] + phase_s[1] + phase_s[2]}, {"TFORM", tform_s},
+      {"SOLVR", phase_s[3]}, {"COLOR", 0.0}, {"TOTAL", wall}};
+  for (const auto& r : rows) std::fprintf(tf, "%-6s%18.6f\n", r.first, r.second);
+  std::fprintf(tf, "Malha e sistema linear:\nPoromecanico:\n");
+  const std::pair<const char*, long long> cnt[] = {
+      {"neq", neq}, {"nad", (long long)nad}, {"nnode", d->nnode}, {"numel", d->numel},
+      {"colors", nc}};
+  for (const auto& r : cnt) std::fprintf(tf, "%-6s%16lld\n", r.first, r.second);
+  std::fclose(tf);
   return PM_OK;
 }
 

@@ -65,6 +65,12 @@ def test_deck_run_matches_golden_histories(golden, tmp_path, name, keys):
     ref = fx["pcg_iters"][:600]
     assert its[0] == ref[0] or abs(its[0] - ref[0]) <= 2
     assert abs(its.mean() - ref.mean()) <= 0.1 * ref.mean()
+    # sizes of the run's log against the reference's _t_1.txt (make_golden.py)
+    with open(prefix + "_t_1.txt") as fh:
+        kv = dict(ln.split()[:2] for ln in fh if len(ln.split()) == 2)
+    assert int(kv["neq"]) == int(fx["neq_ref"]) and int(kv["nad"]) == int(fx["nad_ref"])
+    assert int(kv["nnode"]) == int(fx["nnode_ref"])
+    assert float(kv["SOLVR"]) > 0 and float(kv["TOTAL"]) >= float(kv["SOLVR"])
     assert lines[1].startswith("PCG:  it ")
     assert np.all(np.abs(xkx - fx["pcg_xkx"]) <= 1e-8 * np.abs(fx["pcg_xkx"]) + 1e-13)
 
