@@ -611,31 +611,69 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     PM_TRY(gmres_run(h, d_b, V.x, tol, maxit, &nit, &final_target));
     ks.iter = nit;
   } else if (solver == 11) {
-    if (comp) {
-      h->err = "rpsqmr (solver 11) runs on the FP64 operator (PM_FP64)";
-      return PM_E_ARG;
-    }
-    if (!h->sqmr_graph) {
-      PM_TRY(capture(h, &h->sqmr_graph, [&]() {
-        return pm::sqmr_iteration(P, val64, n, h->D.m, V, h->D.ks, h->D.partial, h->D.counter,
-                                  h->stream);
+    cudaGraphExec_t* g = comp ? &h->sqmrc_graph : &h->sqmr_graph;
+    if (!*g) {
+      PM_TRY(capture(h, g, [&]() {
+        return comp ? pm::sqmrc_iteration(P, C, n, h->D.m, V, V32, h->D.ks, h->D.partial,
+                                          h->D.counter, h->stream)
+                    : pm::sqmr_iteration(P, val64, n, h->D.m, V, h->D.ks, h->D.partial,
+                                         h->D.counter, h->stream);
       }));
     }
+    auto run_sqmr = [&]() -> int {
+      for (;;) {
+        PM_CUDA(cudaGraphLaunch(*g, h->stream));
+        h->launches += 4 * kGraphIters;
+        PM_TRY(read_scalars(h, &ks));
+        if (ks.conv_flag) return PM_OK;
+      }
+    };
     h->launches += 1;
-    PM_CUDA(pm::sqmr_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
-                          h->stream));
-    for (;;) {
-      PM_CUDA(cudaGraphLaunch(h->sqmr_graph, h->stream));
-      h->launches += 4 * kGraphIters;
-      PM_TRY(read_scalars(h, &ks));
-      if (ks.conv_flag) break;
+    PM_CUDA(pm::sqmr_init(n, d_b, h->D.m, V, comp ? V32.c : nullptr, h->D.ks, tol, -1.0, maxit,
+                          h->D.partial, h->D.counter, h->stream));
+    PM_TRY(run_sqmr());
+    int total = ks.iter;
+    const double conv = ks.conv;
+    // compensated operator: the FP64 residual b - A64 x (rpsqmr's 2-norm
+    // test, conv = tol ||b||) decides; a correction sweep solves for it
+    while (comp && ks.conv_flag == 1) {
+      h->launches += 3;
+      if (sweeps == 0) {
+        if (d_x != V.x)
+          PM_CUDA(cudaMemcpyAsync(d_x, V.x, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                  h->stream));
+      } else {
+        PM_CUDA(pm::axpy_into(n, d_x, V.x, 1.0, h->stream));
+      }
+      PM_CUDA(pm::spmv(P, val64, d_x, h->D.dx, 0, nullptr, nullptr, nullptr, h->stream));
+      PM_CUDA(pm::true_residual(n, d_b, h->D.dx, nullptr, 2, h->D.rr, h->D.norms, h->D.partial,
+                                h->D.counter, h->stream));
+      double rn2 = 0.0;
+      PM_CUDA(cudaMemcpyAsync(&rn2, h->D.norms, sizeof(double), cudaMemcpyDeviceToHost,
+                              h->stream));
+      PM_CUDA(cudaStreamSynchronize(h->stream));
+      ++sweeps;
+      if (h->debug)
+        fprintf(stderr, "refine sweep %d: |b-A64x| %.3e target %.3e after %d its\n", sweeps,
+                std::sqrt(std::fabs(rn2)), conv, total);
+      if (std::sqrt(std::fabs(rn2)) < conv) break;
+      if (sweeps >= 8 || total >= maxit) {
+        ks.conv_flag = 2;
+        break;
+      }
+      h->launches += 1;
+      PM_CUDA(pm::sqmr_init(n, h->D.rr, h->D.m, V, V32.c, h->D.ks, tol, conv, maxit - total,
+                            h->D.partial, h->D.counter, h->stream));
+      PM_TRY(run_sqmr());
+      total += ks.iter;
     }
+    ks.iter = total;
     if (ks.conv_flag == 2) {
-      // Solv.f:765: rpsqmr reached maxit; GMRES(l) from x = 0
+      // Solv.f:765: rpsqmr reached maxit; GMRES(l) from x = 0 (FP64 operator)
       const int its = ks.iter;
       int nit = 0;
       if (h->debug) fprintf(stderr, "rpsqmr: maxit reached, switching to GMRES(l)\n");
-      const int st2 = gmres_run(h, d_b, V.x, tol, maxit, &nit, &final_target);
+      const int st2 = gmres_run(h, d_b, comp ? d_x : V.x, tol, maxit, &nit, &final_target);
       if (st2 != PM_OK) {
         if (info) info->iters = its + nit;
         return st2;
@@ -656,7 +694,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
   if (comp && h->shape == pm::kCsShape) PM_TRY(check_cs_fault(h));
   PM_CUDA(cudaEventRecord(e1, h->stream));
   // x.Kx of the solver log (one more product with the converged x)
-  const double* xs = (comp && solver == 1) ? d_x : V.x;
+  const double* xs = (comp && (solver == 1 || solver == 11)) ? d_x : V.x;
   h->launches += 1;
   PM_CUDA(pm::spmv(P, val64, xs, V.q, 3, h->D.ks, h->D.partial, h->D.counter, h->stream));
   if (d_x != xs)
@@ -1191,6 +1229,7 @@ void free_all(Handle* h) {
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
   if (h->pcgc_graph) cudaGraphExecDestroy(h->pcgc_graph);
   if (h->sqmr_graph) cudaGraphExecDestroy(h->sqmr_graph);
+  if (h->sqmrc_graph) cudaGraphExecDestroy(h->sqmrc_graph);
   if (h->bpcg_graph) cudaGraphExecDestroy(h->bpcg_graph);
   if (h->bpcgc_graph) cudaGraphExecDestroy(h->bpcgc_graph);
   for (void* p : {(void*)h->B.eq_ptr, (void*)h->B.blk_ptr, (void*)h->B.blk_inst, (void*)h->B.bs,

@@ -207,6 +207,7 @@ struct Handle {
   cudaGraphExec_t pcgc_graph = nullptr, minresc_graph = nullptr;
   cudaGraphExec_t bpcg_graph = nullptr, bpcgc_graph = nullptr;
   cudaGraphExec_t sqmr_graph = nullptr;
+  cudaGraphExec_t sqmrc_graph = nullptr;
   double timers[8] = {0};
   int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;

@@ -70,9 +70,9 @@ cudaError_t pcg_iteration(const PanelView& P, const double* val64, int n, const 
                           KrylovVecs& V, KrylovScalars* ks, double* partial,
                           unsigned* counter, cudaStream_t s);
 // rpsqmr (Iters.f:6100-6439): init and one iteration (4 launches)
-cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V,
-                      KrylovScalars* ks, double tol, int maxit, double* partial,
-                      unsigned* counter, cudaStream_t s);
+cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V, float2* qc,
+                      KrylovScalars* ks, double tol, double conv_abs, int maxit,
+                      double* partial, unsigned* counter, cudaStream_t s);
 cudaError_t sqmr_iteration(const PanelView& P, const double* val64, int n, const double* m,
                            KrylovVecs& V, KrylovScalars* ks, double* partial,
                            unsigned* counter, cudaStream_t s);
@@ -179,6 +179,9 @@ cudaError_t pcgc_iteration(const PanelView& P, CompVals C, int n, const double* 
 cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const double* m,
                               KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
                               double* partial, unsigned* counter, cudaStream_t s);
+cudaError_t sqmrc_iteration(const PanelView& P, CompVals C, int n, const double* m,
+                            KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                            double* partial, unsigned* counter, cudaStream_t s);
 cudaError_t true_residual(int n, const double* b, const double* q, const double* m, int absval,
                           double* r, double* out, double* partial, unsigned* counter,
                           cudaStream_t s);

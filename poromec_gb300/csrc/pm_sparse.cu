@@ -1215,7 +1215,7 @@ __global__ void __launch_bounds__(256)
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double ri = b[i] - q[i];
     r[i] = ri;
-    acc += ri * ri * (absval ? fabs(m[i]) : m[i]);
+    acc += ri * ri * (absval == 2 ? 1.0 : absval ? fabs(m[i]) : m[i]);
   }
   double in[1] = {acc}, tot[1];
   if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) out[0] = tot[0];
@@ -1232,11 +1232,14 @@ __global__ void __launch_bounds__(256)
 
 // x = 0, r = b (- A 0), q = M r, d = 0; conv = tol ||b||, tau = ||r||,
 // rho = (r, q)
+// qc (compensated operator): the FP32 pair of q as well; conv_abs > 0
+// replaces tol ||b|| (a correction sweep of the refinement aims at the
+// original target)
 __global__ void __launch_bounds__(256)
     k_sqmr_init(int n, const double* __restrict__ b, const double* __restrict__ m,
                 double* __restrict__ r, double* __restrict__ q, double* __restrict__ dv,
-                double* __restrict__ x, KrylovScalars* ks, double tol, int maxit,
-                double* partial, unsigned* counter) {
+                double* __restrict__ x, float2* __restrict__ qc, KrylovScalars* ks, double tol,
+                double conv_abs, int maxit, double* partial, unsigned* counter) {
   double bb = 0.0, rq = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double bi = b[i];
@@ -1244,13 +1247,14 @@ __global__ void __launch_bounds__(256)
     r[i] = bi;
     const double qi = bi * m[i];
     q[i] = qi;
+    if (qc) split_store(qi, qc, i);
     dv[i] = 0.0;
     bb += bi * bi;
     rq += bi * qi;
   }
   double in[2] = {bb, rq}, tot[2];
   if (grid_reduce<2>(in, partial, counter, tot) && threadIdx.x == 0) {
-    ks->conv = tol * sqrt(fabs(tot[0]));
+    ks->conv = conv_abs > 0.0 ? conv_abs : tol * sqrt(fabs(tot[0]));
     ks->normr = sqrt(tot[0]);
     ks->d = tot[1];
     ks->neta = 0.0;
@@ -1324,11 +1328,15 @@ __global__ void __launch_bounds__(256)
 
 // q = t + beta q
 __global__ void __launch_bounds__(256)
-    k_sqmr_dir(int n, const double* __restrict__ t, double* __restrict__ q, KrylovScalars* ks) {
+    k_sqmr_dir(int n, const double* __restrict__ t, double* __restrict__ q,
+               float2* __restrict__ qc, KrylovScalars* ks) {
   if (krylov_skip(ks, false)) return;
   const double beta = ks->beta;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    q[i] = t[i] + beta * q[i];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double qi = t[i] + beta * q[i];
+    q[i] = qi;
+    if (qc) split_store(qi, qc, i);
+  }
 }
 
 // ---- reference CSRD layout --------------------------------------------------
@@ -1482,11 +1490,11 @@ cudaError_t pcg_iteration(const PanelView& P, const double* val64, int n, const 
   return cudaGetLastError();
 }
 
-cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V,
-                      KrylovScalars* ks, double tol, int maxit, double* partial,
-                      unsigned* counter, cudaStream_t s) {
-  k_sqmr_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.r, V.p, V.z, V.x, ks, tol, maxit, partial,
-                                           counter);
+cudaError_t sqmr_init(int n, const double* b, const double* m, KrylovVecs& V, float2* qc,
+                      KrylovScalars* ks, double tol, double conv_abs, int maxit,
+                      double* partial, unsigned* counter, cudaStream_t s) {
+  k_sqmr_init<<<vec_grid(n), 256, 0, s>>>(n, b, m, V.r, V.p, V.z, V.x, qc, ks, tol, conv_abs,
+                                           maxit, partial, counter);
   return cudaGetLastError();
 }
 
@@ -1498,7 +1506,7 @@ cudaError_t sqmr_iteration(const PanelView& P, const double* val64, int n, const
   if (e != cudaSuccess) return e;
   k_sqmr_r<<<vec_grid(n), 256, 0, s>>>(n, V.r, V.q, ks, partial, counter);
   k_sqmr_x<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, V.x, V.r, m, V.q, ks, partial, counter);
-  k_sqmr_dir<<<vec_grid(n), 256, 0, s>>>(n, V.q, V.p, ks);
+  k_sqmr_dir<<<vec_grid(n), 256, 0, s>>>(n, V.q, V.p, nullptr, ks);
   return cudaGetLastError();
 }
 
@@ -1803,6 +1811,19 @@ cudaError_t pcgc_iteration(const PanelView& P, CompVals C, int n, const double* 
   k_pcg_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.p, V.r, V.q, m, V.z, ks, partial,
                                             counter);
   k_pcgc_dir<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, V32.c, ks);
+  return cudaGetLastError();
+}
+
+// rpsqmr on the compensated operator: the product of the FP32 pair of q
+// (same fused sigma and alpha), the FP64 updates, and the direction writing
+// the pair of the new q
+cudaError_t sqmrc_iteration(const PanelView& P, CompVals C, int n, const double* m,
+                            KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
+                            double* partial, unsigned* counter, cudaStream_t s) {
+  launch_spmv_cf<1>(P, C, V32.c, V.q, V.p, ks, partial, counter, s);
+  k_sqmr_r<<<vec_grid(n), 256, 0, s>>>(n, V.r, V.q, ks, partial, counter);
+  k_sqmr_x<<<vec_grid(n), 256, 0, s>>>(n, V.z, V.p, V.x, V.r, m, V.q, ks, partial, counter);
+  k_sqmr_dir<<<vec_grid(n), 256, 0, s>>>(n, V.q, V.p, V32.c, ks);
   return cudaGetLastError();
 }
 

@@ -341,7 +341,8 @@ def test_compensated_spmv_rounding_bound(problems, shape, monkeypatch):
 # MINRES cases: the jittered tetra mesh and the cube; on the golden tetra
 # column MINRES itself stalls (the reference's FP64 MINRES and the oracle
 # need ~8e5 iterations there), which says nothing about the operator
-@pytest.mark.parametrize("solver,precond,cases", [(1, 2, [2, 4]), (7, 5, [3, 4])])
+@pytest.mark.parametrize("solver,precond,cases", [(1, 2, [2, 4]), (7, 5, [3, 4]),
+                                                  (11, 2, [2, 3, 4])])
 def test_compensated_solve_matches_fp64(problems, solver, precond, cases, shape, monkeypatch):
     """The compensated operator inside the FP64 refinement reaches the FP64
     solution: same stopping test, FP64 outer residual."""
@@ -356,21 +357,41 @@ def test_compensated_solve_matches_fp64(problems, solver, precond, cases, shape,
         # maxit is per MINRES cycle (10 restarts, as call_minres): on these small,
         # ill-conditioned tetra meshes the recursion can stall in a cycle, which
         # the next restart (an FP64 residual) resolves
-        cap = 400000 if solver == 1 else 20000
+        cap = 400000 if solver in (1, 11) else 20000
         x64, _ = m.solve(b, solver=solver, precond=precond, tol=tol, maxit=cap)
         m.set_precision(pg.capi.PM_FP32C_REFINE)
         xc, info = m.solve(b, solver=solver, precond=precond, tol=tol, maxit=cap)
         assert info.refine >= 1
         assert np.abs(xc - x64).max() <= 1e4 * tol * np.abs(x64).max()
         # the FP64 residual of the result meets the solver's own test:
-        # sqrt|(r, m r)| < tol sqrt|(b, m b)|, m = 1/ad (PCG) or |1/ad| (MINRES)
+        # sqrt|(r, m r)| < tol sqrt|(b, m b)|, m = 1/ad (PCG) or |1/ad| (MINRES);
+        # rpsqmr: ||r|| < tol ||b|| (Iters.f:6221-6223)
         m.set_precision(pg.capi.PM_FP64)  # matvec follows the precision mode
         r = b - m.matvec(xc)
         _, _, ad, _ = m.get_csrd()
-        w = 1.0 / ad if precond == 2 else np.abs(1.0 / ad)
+        w = np.ones_like(ad) if solver == 11 else 1.0 / ad if precond == 2 else np.abs(1.0 / ad)
         rn = np.sqrt(abs(np.sum(r * r * w)))
         bn = np.sqrt(abs(np.sum(b * b * w)))
         assert rn <= 1.01 * tol * bn, (rn, tol * bn)
+
+
+def test_compensated_rpsqmr_steps_on_tetra():
+    """Steps of the unstructured tetra10 problem with the reference's default
+    solver on the compensated operator stay within 1e-7 relative of the FP64
+    rpsqmr steps (both to 1e-9)."""
+    pb = meshgen.tetra_problem(n=4)
+    m64 = pg.from_problem(pb)
+    mc = pg.from_problem(pb)
+    mc.set_precision(pg.capi.PM_FP32C_REFINE)
+    kw = dict(maxnlit=2, stop_crit=1, solver=11, precond=2, solvtol=1e-9, maxit=200000)
+    for _ in range(3):
+        m64.step(**kw)
+        info = mc.step(**kw)
+        assert info.refine >= 1
+    u64, _, _ = m64.get_state()
+    uc, _, _ = mc.get_state()
+    for sl in (slice(0, 3), slice(3, 4)):
+        assert np.abs(uc[:, sl] - u64[:, sl]).max() <= 1e-7 * np.abs(u64[:, sl]).max()
 
 
 def test_compensated_steps_match_fp64():
