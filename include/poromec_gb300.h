@@ -148,7 +148,8 @@ int pm_spmv(pm_handle h, const double* x, double* y);
  * 2 = GMRES(l) (gmres2, Iters.f:1411-1700; FP64 only; maxit counts cycles of
  * nkrylov iterations, see pm_set_nkrylov),
  * 7 = preconditioned MINRES (Iters.f:3987-4305, 10 restarts),
- * 11 = rpsqmr (Iters.f:6100-6439, the reference's default; FP64 only; where
+ * 11 = rpsqmr (Iters.f:6100-6439, the reference's default; PM_FP64 or
+ * PM_FP32C_REFINE; where
  * it does not converge in maxit it switches to GMRES(l) from x = 0 with maxit
  * cycles, Solv.f:765, and info->iters counts both); precond 2 = diag 1/ad,
  * 5 = |1/ad|
