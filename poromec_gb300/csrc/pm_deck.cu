@@ -20,6 +20,9 @@
 // loop (their runs accept the second nonlinear iteration, i.e. stop_crit 1),
 // and loads of types 39-43 given inline as "type ncomp v1 .. vncomp" (a
 // one-row table whose first column is the time) instead of a file name.
+// Their runs did one solve per step and accepted it whatever maxnlit said, so
+// "maxnlit n" reads as max(n, 2) nonlinear iterations with stop_crit 1.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -797,10 +800,12 @@ bool parse(Reader& r, pm_deck_s* d) {
       }
       for (int k = 0; k < 3; ++k) s.gravity[k] = g[k];
       settings_op(OP_GRAVITY);
-    } else if (m == "maxnlit") {  // older decks: their runs accept the second iteration
+    } else if (m == "maxnlit") {
+      // older decks: their runs did one solve per step and accepted it (also
+      // with maxnlit 1), i.e. the second iteration's check of stop_crit 1
       long n;
       if (w.size() < 2 || !read_int(r, w[1], &n, "maxnlit")) return false;
-      s.maxnlit = (int)n;
+      s.maxnlit = std::max(2, (int)n);
       s.stop_crit = 1;
       settings_op(OP_NL);
     } else if (m == "nl") {

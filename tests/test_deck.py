@@ -38,7 +38,7 @@ def test_linear_deck_reads_back_to_the_fixture(golden, tmp_path, name):
     assert int(d.value("nnode")) == int(fx["nnode"])
     assert int(d.value("nnodev")) == int(fx["nnodev"])
     assert list(pb["print_nodes"]) == list(fx["hist_nodes"])
-    assert pb["dt"] == float(fx["dt"]) and pb["maxnlit"] == int(fx["maxnlit"])
+    assert pb["dt"] == float(fx["dt"]) and pb["maxnlit"] == max(2, int(fx["maxnlit"]))
     assert pb["solver"] == 1 and pb["maxit"] == int(fx["maxit"])
     assert pb["solvtol"] == float(fx["solver_tol"]) and pb["stop_crit"] == 1
     assert np.array_equal(pb["gravity"], fx["gravity"])

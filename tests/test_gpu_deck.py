@@ -75,6 +75,27 @@ def test_deck_run_matches_golden_histories(golden, tmp_path, name, keys):
     assert np.all(np.abs(xkx - fx["pcg_xkx"]) <= 1e-8 * np.abs(fx["pcg_xkx"]) + 1e-13)
 
 
+@pytest.mark.parametrize("name,nsteps,tol", [
+    ("solo1", 3, 1.5e-10),
+    ("solo_cilindro_hexa_1", 5, 1e-9),
+    ("solo_cilindro_tetra_1", 5, 1e-9),
+])
+def test_larger_decks_first_steps(golden, tmp_path, name, nsteps, tol):
+    """The other shipped decks (element loads read from files, cylinders) for
+    their first steps through the deck runner: u and p histories against the
+    reference's, at the oracle's bars for the same decks."""
+    fx = golden(name)
+    path = write_linear_deck(fx, str(tmp_path), name, nsteps=nsteps)
+    prefix = os.path.join(str(tmp_path), name)
+    _, n = Deck(path).run(prefix, fmt="golden")
+    assert n == nsteps
+    for a, node in enumerate(fx["hist_nodes"]):
+        h = read_history("%s_up_node_%d.txt" % (prefix, node))
+        r = fx["hist"][a][:nsteps + 1]
+        assert h.shape == r.shape
+        assert np.abs(h[:, 2:] - r[:, 2:]).max() <= tol, (name, node)
+
+
 def test_printnode_layout(golden, tmp_path):
     """pnup / pnsf in printnode's (i9,10e18.10) rows (Pdata.f:760)."""
     fx = golden("exemplo1_mesh0_t2")
