@@ -277,7 +277,9 @@ int pm_get_timers(pm_handle h, double* t, int n);
  * the mid-side nodes from their edge's vertices (Rdata.f:2337-2544).  Older
  * decks (element codes 7 / 6, "pcg", "maxnlit", inline type-40 loads) are
  * read too.  Files named in the deck are relative to its directory.  On
- * failure pm_deck_error() gives the message with file and line. */
+ * failure pm_deck_error() gives the message with file and line (per thread;
+ * also for the output files of pm_deck_run and the writers; a failure of a
+ * library call inside pm_deck_run is in pm_last_error(h)). */
 typedef struct pm_deck_s* pm_deck;
 int pm_deck_read(const char* path, pm_deck* d);
 const char* pm_deck_error(void);

@@ -64,7 +64,7 @@ struct Op {
   int n = 0;   // loop count
 };
 
-std::string g_err;  // message of the last failed pm_deck_read
+thread_local std::string g_err;  // message of the last failed pm_deck_* call of this thread
 
 bool to_double(const std::string& t, double* v) {
   std::string u = t;
@@ -918,7 +918,10 @@ struct Printer {
     const std::string fn = prefix + "_" + tag + "_node_" + std::to_string(node) + ".txt";
     const bool first = !opened[fn];
     FILE* f = std::fopen(fn.c_str(), first ? "w" : "a");
-    if (!f) return PM_E_ARG;
+    if (!f) {
+      g_err = "cannot write " + fn;
+      return PM_E_ARG;
+    }
     if (first) std::fprintf(f, "# Variacao %s no tempo no ponto%9d\n", name.c_str(), node);
     opened[fn] = true;
     std::fprintf(f, "%9d", istep);
@@ -1085,7 +1088,10 @@ void quad_fill(const pm_deck_s* d, std::vector<double>& a, int gdl) {
 int write_geo(const pm_deck_s* d, const std::string& prefix, bool quad) {
   const std::string fn = prefix + "_bc.vtk";
   FILE* f = std::fopen(fn.c_str(), "w");
-  if (!f) return PM_E_ARG;
+  if (!f) {
+    g_err = "cannot write " + fn;
+    return PM_E_ARG;
+  }
   vtk_head(f, "Geometria lida", false, 0.0, 0);
   int np = 0;
   vtk_mesh(f, d, quad, &np);
@@ -1139,7 +1145,10 @@ int write_res(const pm_deck_s* d, pm_handle h, const std::string& prefix, int is
   }
   const std::string fn = prefix + "_istep_" + std::to_string(istep) + ".vtk";
   FILE* f = std::fopen(fn.c_str(), "w");
-  if (!f) return PM_E_ARG;
+  if (!f) {
+    g_err = "cannot write " + fn;
+    return PM_E_ARG;
+  }
   vtk_head(f, "Malha poro mec", true, t, istep);
   int np = 0;
   vtk_mesh(f, d, quad, &np);
@@ -1270,6 +1279,7 @@ int pm_deck_create(pm_deck d, pm_handle* h) {
 
 int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nsteps) {
   if (!d || !h || !prefix || (format != 0 && format != 1)) return PM_E_ARG;
+  g_err.clear();
   Printer pr{prefix, format, {}};
   Settings s = d->init;
   int istep = 0;
@@ -1326,7 +1336,10 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
         for (int q = 0; q < 4; ++q) phase_s[q] += tm[q] * 1e-3;
         const std::string ln = std::string(prefix) + "_log_1.txt";
         FILE* lf = std::fopen(ln.c_str(), log_open ? "a" : "w");
-        if (!lf) return PM_E_ARG;
+        if (!lf) {
+          g_err = "cannot write " + ln;
+          return PM_E_ARG;
+        }
         if (!log_open) std::fputs("Solver control flop.\n", lf);
         log_open = true;
         static const char* names[] = {"", "PCG:", "GMRES2:", "", "", "", "", "MINRES:", "", "",
@@ -1403,7 +1416,10 @@ int pm_deck_run(pm_deck d, pm_handle h, const char* prefix, int format, int* nst
       std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
   const std::string tn = std::string(prefix) + "_t_1.txt";
   FILE* tf = std::fopen(tn.c_str(), "w");
-  if (!tf) return PM_E_ARG;
+  if (!tf) {
+    g_err = "cannot write " + tn;
+    return PM_E_ARG;
+  }
   std::fprintf(tf, "# Arquivo de log do poro mecanico\nTempos (seg):\n"
                    "Resolucao do tempo:  1.00E-06\n");
   const std::pair<const char*, double> rows[] = {

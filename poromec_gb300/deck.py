@@ -115,7 +115,7 @@ class Deck:
         """<prefix>_bc.vtk: the mesh as read (the pgeo macro)."""
         st = self.lib.pm_deck_write_geo(self.d, os.fspath(prefix).encode(), int(bool(quad)))
         if st != 0:
-            raise DeckError("cannot write %s_bc.vtk" % prefix)
+            raise DeckError(self.lib.pm_deck_error().decode())
         return os.fspath(prefix) + "_bc.vtk"
 
     def write_res(self, mesh, prefix, istep, t, quad=True, fields=0x3F):
@@ -137,7 +137,8 @@ class Deck:
         st = self.lib.pm_deck_run(self.d, m.h, os.fspath(prefix).encode(),
                                   {"printnode": 0, "golden": 1}[fmt], ctypes.byref(n))
         if st != 0:
-            raise capi.PMError(st, "pm_deck_run", m.lib.pm_last_error(m.h).decode())
+            detail = self.lib.pm_deck_error().decode() or m.lib.pm_last_error(m.h).decode()
+            raise capi.PMError(st, "pm_deck_run", detail)
         return m, n.value
 
 
