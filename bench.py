@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=2,
                     help="timed steps of the batch leg in the default run")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-tetra", action="store_true",
+                    help="leave out the unstructured tetra10 leg of the default run")
     ap.add_argument("--fp32-plain", action="store_true",
                     help="also time the plain FP32-value refinement (PM_FP32_REFINE)")
     ap.add_argument("--spmv-only", action="store_true",
@@ -399,7 +401,7 @@ def run_adjoint(args):
         flush=True)
 
 
-def run_tetra(args):
+def tetra_leg(args, steps, warmup):
     """Unstructured tetra10 workload: --tetra-n^3 hex cells on a 2 x 2 x 1 m box
     split in 6 Kuhn tets, interior vertices jittered, two layers, a point
     source, dt 60 s.  Solver: rpsqmr (solver 11, the reference's default) with
@@ -417,19 +419,19 @@ def run_tetra(args):
     dt = float(pb["dt"])
     kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=11, precond=2,
               solvtol=float(pb.get("solvtol", 1e-8)), maxit=200000, reassemble=True)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         m.step(**kw)
     snap = m.get_state()
 
     def restore():
         m.set_state(*snap)
-        m.set_env(pb["gravity"], dt, args.warmup * dt, args.warmup)
+        m.set_env(pb["gravity"], dt, warmup * dt, warmup)
 
     def timed():
         its = []
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             its.append(m.step(**kw).iters)
         torch.cuda.synchronize()
         return time.perf_counter() - t0, its
@@ -446,20 +448,30 @@ def run_tetra(args):
         uc, _, _ = m.get_state()
     du = float(np.abs(uc[:, :3] - u64[:, :3]).max() / np.abs(u64[:, :3]).max())
     dp_ = float(np.abs(uc[:, 3] - u64[:, 3]).max() / np.abs(u64[:, 3]).max())
+    neq, nad, shape = m.neq, m.nad, m.tune_spmv()
+    m.close()
+    return {"value": steps / t64, "unit": "steps/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": t64 / steps * 1e3,
+            "workload": "tetra10 Kuhn %d^3 on 2x2x1 m, %d equations, nad %d, rpsqmr tol %g, "
+                        "K re-assembled every step" % (args.tetra_n, neq, nad, kw["solvtol"]),
+            "iterations_per_step": its64,
+            "fp32_refine": {"value": steps / tc, "unit": "steps/s",
+                            "speedup_vs_fp64": t64 / tc, "shape": shape,
+                            "iterations_per_step": itsc,
+                            "rel_err_vs_fp64_same_tol": {"u": du, "p": dp_}},
+            "clocks": clk.summary()}
+
+
+def run_tetra(args):
+    t = tetra_leg(args, args.steps, args.warmup)
     out = {"metric": "Biot steps/s, unstructured tetra10 rpsqmr: FP64 plain vs FP32+refine",
-           "value": args.steps / t64, "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": t64 / args.steps * 1e3,
+           "value": t["value"], "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t["ms_per_step"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded jitter, two layers, point source)",
-           "config": {"workload": "tetra10 Kuhn %d^3 on 2x2x1 m, %d equations, nad %d, rpsqmr "
-                                  "tol %g, K re-assembled every step" % (
-                                      args.tetra_n, m.neq, m.nad, kw["solvtol"]),
-                      "iterations_per_step": its64},
-           "fp32_refine": {"value": args.steps / tc, "unit": "steps/s",
-                           "speedup_vs_fp64": t64 / tc, "shape": m.tune_spmv(),
-                           "iterations_per_step": itsc,
-                           "rel_err_vs_fp64_same_tol": {"u": du, "p": dp_}},
-           "clocks": clk.summary()}
+           "config": {"workload": t["workload"],
+                      "iterations_per_step": t["iterations_per_step"]},
+           "fp32_refine": t["fp32_refine"], "clocks": t["clocks"]}
     print(json.dumps(out), flush=True)
 
 
@@ -644,6 +656,8 @@ def run_gpu(args):
     if not args.no_batch:
         m.close()  # the batch needs the memory more than the finished cube
         out["batched"] = batched_leg(args, args.batch_steps, 1)
+    if not args.no_tetra:
+        out["tetra"] = tetra_leg(args, 2, 1)
     if not args.no_cpu:
         t_step, parts, sample, threads = cpu_step_estimate(pb, int(np.mean(iters)))
         out["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads,
