@@ -1518,6 +1518,7 @@ static int mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int 
   };
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(PM_E_CUDA);
+  if (pm::ensure_shape_tables() != cudaSuccess) return fail(PM_E_CUDA);
   for (auto& ev : h->ev)
     if (cudaEventCreate(&ev) != cudaSuccess) return fail(PM_E_CUDA);
   if ((st = pm::build_structure(h, ix, id, fnno, x, num)) != PM_OK) return fail(st);

@@ -17,8 +17,12 @@
 // which is the reference's per-point 9-entry update regrouped (the same
 // products, summed in a different order).  The blocks are added straight
 // into the node panels; elements of one colour share no node, so the adds
-// need no atomics.
+// need no atomics.  The hexa's shape functions at its 64 points come from a
+// table filled once per device (ensure_shape_tables); each point's values
+// are scaled by sqrt(w_g) before the pair loops, so these need no w_g.
 #include <cuda_runtime.h>
+
+#include <mutex>
 
 #include "pm_internal.h"
 
@@ -183,23 +187,112 @@ struct Geo {
   T xv[NV][3];
 };
 
+// Shape functions of the hexa at its 64 integration points are the same for
+// every element: a table filled once per device by k_fill_shape_tables from
+// the sf_* functions above, so its values are theirs bit for bit.  Row k
+// holds one function at the 64 points, so a warp's loads are coalesced.
+constexpr int kTabH8 = 0;     // rows 0..31: h, hr, hs, ht of sfhexa8 (8 each)
+constexpr int kTabH20D = 32;  // rows 32..91: hr, hs, ht of sfhexa20 (20 each)
+constexpr int kTabH20V = 92;  // rows 92..111: h of sfhexa20
+constexpr int kTabRows = 112;
+constexpr int kHexaGp = 64;
+__device__ double gShapeHexa[kTabRows * kHexaGp];
+
+__global__ void k_fill_shape_tables() {
+  const int gq = threadIdx.x;
+  if (gq >= kHexaGp) return;
+  const int lz = gq >> 4, ly = (gq >> 2) & 3, lx = gq & 3;
+  const double r = cPG4[lx], s = cPG4[ly], t = cPG4[lz];
+  double h[8], hr[8], hs[8], ht[8], ur[20], us[20], ut[20], hv[20];
+  sf_hexa8<double>(r, s, t, h, hr, hs, ht);
+  sf_hexa20_d<double>(r, s, t, ur, us, ut);
+  sf_hexa20_v<double>(r, s, t, hv);
+  double* tb = gShapeHexa + gq;
+  for (int k = 0; k < 8; ++k) {
+    tb[(kTabH8 + k) * kHexaGp] = h[k];
+    tb[(kTabH8 + 8 + k) * kHexaGp] = hr[k];
+    tb[(kTabH8 + 16 + k) * kHexaGp] = hs[k];
+    tb[(kTabH8 + 24 + k) * kHexaGp] = ht[k];
+  }
+  for (int k = 0; k < 20; ++k) {
+    tb[(kTabH20D + k) * kHexaGp] = ur[k];
+    tb[(kTabH20D + 20 + k) * kHexaGp] = us[k];
+    tb[(kTabH20D + 40 + k) * kHexaGp] = ut[k];
+    tb[(kTabH20V + k) * kHexaGp] = hv[k];
+  }
+}
+
 // Integration point geometry (thread-per-point).  Returns false when the
 // determinant is <= 1e-14, the condition jacob3d_m stops on.
 template <bool HEXA, typename T>
 __device__ bool point_geometry_rst(Geo<HEXA, T>& G, int gq, T r, T s, T t, T wq, T* huv);
 
+// The hexa's point geometry from the shape tables: the Jacobian from the
+// vertices, its inverse by one reciprocal of the determinant, and the
+// physical derivatives, with the table rows streamed from L1.
+template <typename T>
+__device__ bool point_geometry_hexa_tab(Geo<true, T>& G, int gq, T* huv) {
+  constexpr int NEN = 20, NV = 8;
+  const double* tb = gShapeHexa + gq;
+  auto tab = [tb](int row) { return T(__ldg(tb + row * kHexaGp)); };
+  T J[3][3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    T a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const T xk = G.xv[k][j];
+      a0 += tab(kTabH8 + 8 + k) * xk;
+      a1 += tab(kTabH8 + 16 + k) * xk;
+      a2 += tab(kTabH8 + 24 + k) * xk;
+    }
+    J[0][j] = a0; J[1][j] = a1; J[2][j] = a2;
+  }
+  const T det = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] +
+                J[0][2] * J[1][0] * J[2][1] - J[2][0] * J[1][1] * J[0][2] -
+                J[1][0] * J[0][1] * J[2][2] - J[0][0] * J[2][1] * J[1][2];
+  if (!(det > T(1.0e-14))) return false;
+  const T rd = T(1) / det;
+  T Ji[3][3];
+  Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * rd;
+  Ji[1][0] = -(J[1][0] * J[2][2] - J[1][2] * J[2][0]) * rd;
+  Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * rd;
+  Ji[0][1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * rd;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * rd;
+  Ji[2][1] = -(J[0][0] * J[2][1] - J[0][1] * J[2][0]) * rd;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * rd;
+  Ji[1][2] = -(J[0][0] * J[1][2] - J[0][2] * J[1][0]) * rd;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * rd;
+  const int lz = gq >> 4, ly = (gq >> 2) & 3, lx = gq & 3;
+  G.w[gq] = T(cWG4[lx] * cWG4[ly] * cWG4[lz]) * det;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const T hr = tab(kTabH8 + 8 + k), hs = tab(kTabH8 + 16 + k), ht = tab(kTabH8 + 24 + k);
+    G.hp[gq][k] = tab(kTabH8 + k);
+    G.gp[gq][k][0] = Ji[0][0] * hr + Ji[0][1] * hs + Ji[0][2] * ht;
+    G.gp[gq][k][1] = Ji[1][0] * hr + Ji[1][1] * hs + Ji[1][2] * ht;
+    G.gp[gq][k][2] = Ji[2][0] * hr + Ji[2][1] * hs + Ji[2][2] * ht;
+  }
+#pragma unroll 4
+  for (int k = 0; k < NEN; ++k) {
+    const T ur = tab(kTabH20D + k), us = tab(kTabH20D + 20 + k), ut = tab(kTabH20D + 40 + k);
+    G.g[gq][k][0] = Ji[0][0] * ur + Ji[0][1] * us + Ji[0][2] * ut;
+    G.g[gq][k][1] = Ji[1][0] * ur + Ji[1][1] * us + Ji[1][2] * ut;
+    G.g[gq][k][2] = Ji[2][0] * ur + Ji[2][1] * us + Ji[2][2] * ut;
+  }
+  if (huv)
+    for (int k = 0; k < NEN; ++k) huv[k] = tab(kTabH20V + k);
+  return true;
+}
+
 template <bool HEXA, typename T>
 __device__ bool point_geometry(Geo<HEXA, T>& G, int gq, T* huv) {
-  T r, s, t, wq;
-  if (HEXA) {
-    const int lz = gq >> 4, ly = (gq >> 2) & 3, lx = gq & 3;
-    r = T(cPG4[lx]); s = T(cPG4[ly]); t = T(cPG4[lz]);
-    wq = T(cWG4[lx] * cWG4[ly] * cWG4[lz]);
+  if constexpr (HEXA) {
+    return point_geometry_hexa_tab<T>(G, gq, huv);
   } else {
-    r = T(cPRI4[gq]); s = T(cPSI4[gq]); t = T(cPTI4[gq]);
-    wq = T(0.25);
+    return point_geometry_rst<HEXA, T>(G, gq, T(cPRI4[gq]), T(cPSI4[gq]), T(cPTI4[gq]),
+                                       T(0.25), huv);
   }
-  return point_geometry_rst<HEXA, T>(G, gq, r, s, t, wq, huv);
 }
 
 // The geometry of point (r, s, t) with quadrature weight wq into slot gq of G
@@ -297,6 +390,14 @@ __device__ __forceinline__ void add_val(double* v64, float* v32, int64_t a, T v)
 // ---------------------------------------------------------------------------
 // isw = 2, lhs: element matrix into the panels.
 // ---------------------------------------------------------------------------
+// The weight a pair loop still applies at point gq: none for the hexa, whose
+// point values k_assemble_K scales by sqrt(w); w for the tetra.
+template <bool HEXA, typename T>
+__device__ __forceinline__ T pair_weight(const Geo<HEXA, T>& G, int gq) {
+  if constexpr (HEXA) return T(1);
+  else return G.w[gq];
+}
+
 template <bool HEXA, typename T>
 struct SmK {
   Geo<HEXA, T> G;
@@ -331,8 +432,28 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     }
     sE0[k] = e0;
   }
-  for (int gq = threadIdx.x; gq < NGP; gq += NT)
-    if (!point_geometry<HEXA, T>(G, gq, nullptr)) sFail = 1;
+  for (int gq = threadIdx.x; gq < NGP; gq += NT) {
+    if (!point_geometry<HEXA, T>(G, gq, nullptr)) {
+      sFail = 1;
+      continue;
+    }
+    // every entry below is a sum over points of w times a product of two
+    // point values: for the hexa's 64 points, scale the point's values by
+    // sqrt(w) (w > 0 here) and the pair loops need no multiply by w; the
+    // tetra's 4-point loops keep the per-pair weight
+    if constexpr (HEXA) {
+      const T sw = sqrt(G.w[gq]);
+#pragma unroll
+      for (int k = 0; k < NEN; ++k) {
+        G.g[gq][k][0] *= sw; G.g[gq][k][1] *= sw; G.g[gq][k][2] *= sw;
+      }
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        G.hp[gq][k] *= sw;
+        G.gp[gq][k][0] *= sw; G.gp[gq][k][1] *= sw; G.gp[gq][k][2] *= sw;
+      }
+    }
+  }
   __syncthreads();
   if (sFail) {
     if (threadIdx.x == 0) atomicOr(L.err, 1);
@@ -352,7 +473,7 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     T P[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
 #pragma unroll 4
     for (int gq = 0; gq < NGP; ++gq) {
-      const T w = G.w[gq];
+      const T w = pair_weight(G, gq);
       const T gi0 = w * G.g[gq][i][0], gi1 = w * G.g[gq][i][1], gi2 = w * G.g[gq][i][2];
       const T gj0 = G.g[gq][j][0], gj1 = G.g[gq][j][1], gj2 = G.g[gq][j][2];
       P[0][0] += gi0 * gj0; P[0][1] += gi0 * gj1; P[0][2] += gi0 * gj2;
@@ -396,7 +517,7 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     T A0 = 0, A1 = 0, A2 = 0;
 #pragma unroll 4
     for (int gq = 0; gq < NGP; ++gq) {
-      const T wh = G.w[gq] * G.hp[gq][l];
+      const T wh = pair_weight(G, gq) * G.hp[gq][l];
       A0 += wh * G.g[gq][j][0]; A1 += wh * G.g[gq][j][1]; A2 += wh * G.g[gq][j][2];
     }
     const T Kv[3] = {-alpha * A0, -alpha * A1, -alpha * A2};
@@ -421,14 +542,21 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
     int l = 0;
     while ((l + 1) * (l + 2) / 2 <= pr) ++l;
     const int m = pr - l * (l + 1) / 2;
-    T acc = 0;
+    T acc = 0, am = 0, ak = 0;
 #pragma unroll 4
     for (int gq = 0; gq < NGP; ++gq) {
-      const T w = G.w[gq];
-      acc += w * imod * G.hp[gq][l] * G.hp[gq][m] +
-             w * dtp * (G.gp[gq][l][0] * G.gp[gq][m][0] + G.gp[gq][l][1] * G.gp[gq][m][1] +
-                        G.gp[gq][l][2] * G.gp[gq][m][2]);
+      if constexpr (HEXA) {  // values carry sqrt(w)
+        am += G.hp[gq][l] * G.hp[gq][m];
+        ak += G.gp[gq][l][0] * G.gp[gq][m][0] + G.gp[gq][l][1] * G.gp[gq][m][1] +
+              G.gp[gq][l][2] * G.gp[gq][m][2];
+      } else {
+        const T w = G.w[gq];
+        acc += w * imod * G.hp[gq][l] * G.hp[gq][m] +
+               w * dtp * (G.gp[gq][l][0] * G.gp[gq][m][0] + G.gp[gq][l][1] * G.gp[gq][m][1] +
+                          G.gp[gq][l][2] * G.gp[gq][m][2]);
+      }
     }
+    if constexpr (HEXA) acc = imod * am + dtp * ak;
     const int er = sEq[l][3], ec = sEq[m][3];
     if (er == 0 || ec == 0) continue;
     const int nl = E.nodes[l], nm = E.nodes[m];
@@ -1211,6 +1339,26 @@ cudaError_t launch_elem(Kern k, int n, int nt, cudaStream_t s, Args... args) {
 }
 
 }  // namespace
+
+cudaError_t ensure_shape_tables() {
+  static std::mutex mu;
+  static bool filled[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (filled[dev]) return cudaSuccess;
+  cudaStream_t s;
+  if ((e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  k_fill_shape_tables<<<1, kHexaGp, 0, s>>>();
+  e = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) filled[dev] = true;
+  return e;
+}
 
 cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val64,
                               float* val32, cudaStream_t s) {

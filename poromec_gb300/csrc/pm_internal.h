@@ -94,6 +94,10 @@ struct ElemLaunch {
   int* err;
 };
 
+// The hexa shape-function table of the element kernels, filled once per
+// device; called before a handle's first element launch.
+constexpr int kMaxDevices = 64;
+cudaError_t ensure_shape_tables();
 cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val64,
                               float* val32, cudaStream_t s);
 cudaError_t launch_residual(const ElemLaunch& L, bool hexa, const double* u,
