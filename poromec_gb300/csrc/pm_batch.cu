@@ -59,8 +59,7 @@ __device__ bool seg_reduce(const BatchView& B, int inst, const double (&v)[NV],
 }
 
 __device__ __forceinline__ void pair_store(double v, float2* pr, int i) {
-  const float h = float(v);
-  pr[i] = make_float2(h, float(v - double(h)));
+  pr[i] = split_pair(v);
 }
 
 // x = 0, r = b, z = m r, p = z, d = (r, z); conv = tol sqrt|d| (pcg's test)

@@ -5,6 +5,37 @@
 
 namespace pm {
 
+#ifdef __CUDACC__
+// v as an unevaluated FP32 pair (hi, lo), the operand format of the
+// compensated operator, split by truncation on the integer pipe: hi keeps
+// the top 24 significand bits of v and lo the top 24 of the exact remainder
+// v - hi, so |v - hi - lo| < 2^-46 |v|.  For 2^-78 <= |v| < 2^127 both are
+// built from v's bits (lo = 0 where the remainder is below float's normal
+// range, an error under 2^-47 |v|), with no FP64 conversion; other values
+// take the rounded conversions.
+__device__ __forceinline__ float2 split_pair(double v) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(v));
+  const unsigned e = unsigned(b >> 52) & 0x7ffu;  // biased FP64 exponent
+  if (e - 945u <= 1150u - 945u) {
+    const unsigned sign = unsigned(b >> 32) & 0x80000000u;
+    const float hi = __uint_as_float(sign | ((e - 896u) << 23) | (unsigned(b >> 29) & 0x7fffffu));
+    const unsigned m = unsigned(b) & 0x1fffffffu;  // the 29 significand bits below hi
+    float lo = 0.f;
+    if (m != 0u) {
+      const int k = 31 - __clz(static_cast<int>(m));  // leading bit of m, 0..28
+      const int ef = int(e) - 948 + k;                 // float exponent field of lo
+      if (ef >= 1) {
+        const unsigned mant = k >= 23 ? (m >> (k - 23)) : (m << (23 - k));
+        lo = __uint_as_float(sign | (unsigned(ef) << 23) | (mant & 0x7fffffu));
+      }
+    }
+    return make_float2(hi, lo);
+  }
+  const float h = float(v);
+  return make_float2(h, float(v - double(h)));
+}
+#endif
+
 // Grid of the SpMV and reduction kernels: 8 CTAs of 256 threads per SM on
 // the 152 SMs of a GB300, so the last-block reductions sum at most 1216
 // partials.

@@ -36,12 +36,10 @@ __device__ __forceinline__ bool krylov_skip(KrylovScalars* ks, bool first) {
   return false;
 }
 
-// v as an unevaluated FP32 pair (hi, lo), |v - hi - lo| <= 2^-48 |v|: the
-// operand format of the compensated operator, interleaved so that one 8-byte
-// gather fetches both halves.
+// v as an FP32 pair (split_pair), interleaved so that one 8-byte gather of
+// the compensated operator fetches both halves.
 __device__ __forceinline__ void split_store(double v, float2* pr, int i) {
-  const float h = float(v);
-  pr[i] = make_float2(h, float(v - double(h)));
+  pr[i] = split_pair(v);
 }
 
 // ---- SpMV over panels ------------------------------------------------------
