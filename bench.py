@@ -96,6 +96,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def fp64_peak(torch):
+    """GB300's FP64 pipe: 2 DFMA (4 flops) per SM per clock at the measured
+    maximum SM clock; there is no measured FP64 peak to use instead."""
+    mhz, src = 2070.0, "nominal max SM clock 2070 MHz"
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        if "sm_max_mhz" in d:
+            mhz, src = float(d["sm_max_mhz"]), "MEASURED_PEAKS sm_max_mhz"
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return 4.0 * sms * mhz * 1e6 / 1e12, "2 DFMA per SM per clock x %d SMs x %s" % (sms, src)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -620,6 +633,8 @@ def run_gpu(args):
     B = spmv_bytes(m.nad, m.neq)
     achieved = B / (spmv_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    f64_peak, f64_src = fp64_peak(torch)
+    f64_achieved = 2.0 * m.nnz_panel / (spmv_ms * 1e-3) / 1e12
     traffic = profile_traffic(m.nnz_panel)
     tm = np.mean(np.array(timers), 0)
 
@@ -645,7 +660,11 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
                      "kernel": "k_spmv<double> (node panels)", "launch_ms": spmv_ms,
-                     "algorithmic_bytes": B, "traffic": traffic},
+                     "algorithmic_bytes": B, "traffic": traffic,
+                     # the kernel's actual bound: one DFMA per stored panel value
+                     "fp64_pipe": {"achieved_tflops": f64_achieved, "peak_tflops": f64_peak,
+                                   "frac": f64_achieved / f64_peak, "peak_source": f64_src,
+                                   "flops": 2.0 * m.nnz_panel}},
         "gpu_launches": int(round(args.steps * tm[7])),
         "clocks": clk.summary(),
     }
