@@ -174,7 +174,9 @@ int check_elem_err(Handle* h) {
 }
 
 // isw = 2 with lhs: K into the panels (FP64, and FP32 when refining).
-int assemble_K(Handle* h, bool fp32) {
+// isw 2 with lhs: the panels; with b also rhs (b -= K_e u_e) in the same
+// element launch.
+int assemble_K(Handle* h, bool fp32, const double* u = nullptr, double* b = nullptr) {
   if (fp32) {
     if (!h->P.val32) {
       PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
@@ -190,7 +192,8 @@ int assemble_K(Handle* h, bool fp32) {
   h->launches += h->numcolors;
   for (int c = 0; c < h->numcolors; ++c)
     PM_CUDA(pm::launch_assemble_K(elem_launch(h, c), h->hexa, fp32 ? nullptr : h->P.val,
-                                  fp32 ? h->P.val32 : nullptr, h->stream));
+                                  fp32 ? h->P.val32 : nullptr, h->stream, u,
+                                  fp32 ? nullptr : b));
   if (fp32) {
     h->assembled32 = true;
   } else {
@@ -1348,10 +1351,11 @@ int step_batch(Handle* h, int maxnlit, double tol, int stop_crit, int solver, in
     PM_CUDA(cudaEventRecord(ev[2], s));
     const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
     if (need_K) {
-      PM_TRY(assemble_K(h, false));
+      PM_TRY(assemble_K(h, false, D.u, D.b));  // b -= K u in the same launch
       h->assembled32 = h->assembledC = false;
+    } else {
+      PM_TRY(residual(h, D.u, D.b));
     }
-    PM_TRY(residual(h, D.u, D.b));
     PM_CUDA(cudaEventRecord(ev[3], s));
     PM_TRY(check_elem_err(h));
     float ms = 0.f;
@@ -1750,8 +1754,13 @@ int pm_assemble(pm_handle hh, int isw, int lhs, int rhs, const double* u, double
     PM_CUDA(cudaMemcpyAsync(h->D.by, b, sizeof(double) * h->neq, cudaMemcpyHostToDevice,
                             h->stream));
   if (isw == 2) {
-    if (lhs) PM_TRY(assemble_K(h, false));
-    if (rhs) PM_TRY(residual(h, h->D.bx, h->D.by));
+    if (lhs && rhs) {
+      PM_TRY(assemble_K(h, false, h->D.bx, h->D.by));
+    } else if (lhs) {
+      PM_TRY(assemble_K(h, false));
+    } else if (rhs) {
+      PM_TRY(residual(h, h->D.bx, h->D.by));
+    }
   } else if (rhs) {
     PM_TRY(rhs4(h, h->D.bx, h->D.by));
   }
@@ -1864,11 +1873,11 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
     PM_CUDA(cudaEventRecord(ev[2], s));
     const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
     if (need_K) {
-      PM_TRY(assemble_K(h, false));
+      PM_TRY(assemble_K(h, false, D.u, D.b));  // b -= K u in the same launch
       h->assembled32 = h->assembledC = false;
     }
     PM_CUDA(cudaEventRecord(ev[3], s));
-    PM_TRY(residual(h, D.u, D.b));
+    if (!need_K) PM_TRY(residual(h, D.u, D.b));
     PM_CUDA(cudaEventRecord(ev[4], s));
     PM_TRY(check_elem_err(h));
     float ms = 0.f;

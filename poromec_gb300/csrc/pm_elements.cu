@@ -22,7 +22,11 @@
 // are scaled by sqrt(w_g) before the pair loops, so these need no w_g.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
+#include <type_traits>
+#include <utility>
+#include <vector>
 
 #include "pm_internal.h"
 
@@ -400,18 +404,34 @@ __device__ __forceinline__ T pair_weight(const Geo<HEXA, T>& G, int gq) {
 
 template <bool HEXA, typename T>
 struct SmK {
+  static constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV, NST = 3 * NEN + NV,
+                       NSLOT = NEN + NV;
   Geo<HEXA, T> G;
   ElemCtx E;
-  int sEq[ET<HEXA>::NEN][kNdf];  // equation numbers of the local dofs
-  int sE0[ET<HEXA>::NEN];        // first equation of each node
+  int sEq[NEN][kNdf];  // equation numbers of the local dofs
+  int sE0[NEN];        // first equation of each node
   int sFail;
+  // with RHS: the element's dof values, and (tetra) the contribution slots;
+  // the hexa's slots reuse G.g once the pair loops have read it
+  double ul[NST];
+  double Cx[HEXA ? 1 : NST * NSLOT];
 };
 
-template <bool HEXA, typename T>
+// Element matrix into the panels; with RHS also b -= K_e u_e from the same
+// blocks (p = s.u, the product the reference forms in lku for isw 2 with
+// rhs), one pass instead of a second matrix-free element pass.  The product
+// is deterministic: every block writes its share of a row into a slot of its
+// own (row r of the element vector: slot j for node j's u columns, slot
+// NEN + l for vertex l's p column) and each row sums its slots in order.
+template <bool HEXA, typename T, bool RHS>
 __global__ void __launch_bounds__(ET<HEXA>::NT)
-    k_assemble_K(ElemLaunch L, double* val64, float* val32) {
+    k_assemble_K(ElemLaunch L, double* val64, float* val32, const double* __restrict__ u,
+                 double* __restrict__ bvec) {
   constexpr int NEN = ET<HEXA>::NEN, NV = ET<HEXA>::NV, NGP = ET<HEXA>::NGP,
                 NT = ET<HEXA>::NT;
+  constexpr int NST = SmK<HEXA, T>::NST, NSLOT = SmK<HEXA, T>::NSLOT;
+  static_assert(!RHS || std::is_same<T, double>::value, "the fused product is FP64");
+  static_assert(!HEXA || NST * NSLOT <= NGP * NEN * 3, "hexa slots fit in G.g");
   extern __shared__ __align__(16) unsigned char smem[];
   SmK<HEXA, T>& S = *reinterpret_cast<SmK<HEXA, T>*>(smem);
   Geo<HEXA, T>& G = S.G;
@@ -419,6 +439,7 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
   auto& sEq = S.sEq;
   auto& sE0 = S.sE0;
   int& sFail = S.sFail;
+  const double* ul = S.ul;
   const int el = L.elems[blockIdx.x];
   if (threadIdx.x == 0) sFail = 0;
   load_element<HEXA, T>(L, el, E, G);
@@ -431,6 +452,13 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
       if (e > 0 && e < e0) e0 = e;
     }
     sE0[k] = e0;
+  }
+  if constexpr (RHS) {
+    for (int k = threadIdx.x; k < NST; k += NT) {
+      const int n = k < 3 * NEN ? E.nodes[k / 3] : E.nodes[k - 3 * NEN];
+      const int q = k < 3 * NEN ? k % 3 : 3;
+      S.ul[k] = u[(size_t)kNdf * (n - 1) + q];
+    }
   }
   for (int gq = threadIdx.x; gq < NGP; gq += NT) {
     if (!point_geometry<HEXA, T>(G, gq, nullptr)) {
@@ -463,8 +491,14 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
   const T a = T(mc.a), b = T(mc.b), c = T(mc.c);
   const int32_t* slot = L.slot + (size_t)NEN * NEN * blockIdx.x;
   // ---- Kuu: node pairs (i >= j) -------------------------------------------
-  constexpr int NPAIR = NEN * (NEN + 1) / 2;
-  for (int pr = threadIdx.x; pr < NPAIR; pr += NT) {
+  constexpr int NPAIR = NEN * (NEN + 1) / 2, QUU = (NPAIR + NT - 1) / NT;
+  // RHS: per pair, row (i, k) gets K_ij u_j (slot j) and, for i != j, row
+  // (j, l) gets K_ij^T u_i (slot i); held here until G.g is free
+  double ru[RHS ? QUU : 1][6];
+#pragma unroll
+  for (int q = 0; q < QUU; ++q) {
+    const int pr = threadIdx.x + q * NT;
+    if (pr >= NPAIR) break;
     // decode pr -> (i, j), i >= j
     int i = int((sqrtf(8.0f * pr + 1.0f) - 1.0f) * 0.5f);
     while ((i + 1) * (i + 2) / 2 <= pr) ++i;
@@ -488,6 +522,13 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
       for (int l = 0; l < 3; ++l)
         K[k][l] = (k == l) ? a * (P[k][k] + c * (tr - P[k][k]))
                            : a * (b * P[k][l] + c * P[l][k]);
+    if constexpr (RHS) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        ru[q][k] = K[k][0] * ul[3 * j] + K[k][1] * ul[3 * j + 1] + K[k][2] * ul[3 * j + 2];
+        ru[q][3 + k] = K[0][k] * ul[3 * i] + K[1][k] * ul[3 * i + 1] + K[2][k] * ul[3 * i + 2];
+      }
+    }
     const int ni = E.nodes[i], nj = E.nodes[j];
     const int64_t offi = L.node_val_off[ni - 1], offj = L.node_val_off[nj - 1];
     const int Wi = L.node_W[ni - 1], Wj = L.node_W[nj - 1];
@@ -512,7 +553,14 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
   }
   // ---- Kpu / Kup: (vertex l, node j) ---------------------------------------
   const T alpha = T(mc.coef_biot);
-  for (int pr = threadIdx.x; pr < NV * NEN; pr += NT) {
+  constexpr int NPU = NV * NEN, QPU = (NPU + NT - 1) / NT;
+  // RHS: p row l gets Kpu_lj . u_j (slot j), rows (j, k) get Kup_jl p_l
+  // (slot NEN + l)
+  double rk[RHS ? QPU : 1][4];
+#pragma unroll
+  for (int q = 0; q < QPU; ++q) {
+    const int pr = threadIdx.x + q * NT;
+    if (pr >= NPU) break;
     const int l = pr / NEN, j = pr % NEN;
     T A0 = 0, A1 = 0, A2 = 0;
 #pragma unroll 4
@@ -521,6 +569,11 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
       A0 += wh * G.g[gq][j][0]; A1 += wh * G.g[gq][j][1]; A2 += wh * G.g[gq][j][2];
     }
     const T Kv[3] = {-alpha * A0, -alpha * A1, -alpha * A2};
+    if constexpr (RHS) {
+      const double pl = ul[3 * NEN + l];
+      rk[q][0] = Kv[0] * ul[3 * j] + Kv[1] * ul[3 * j + 1] + Kv[2] * ul[3 * j + 2];
+      rk[q][1] = Kv[0] * pl; rk[q][2] = Kv[1] * pl; rk[q][3] = Kv[2] * pl;
+    }
     const int er = sEq[l][3];
     if (er == 0) continue;
     const int nl = E.nodes[l], nj = E.nodes[j];
@@ -533,6 +586,36 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
       if (ec == 0) continue;
       add_val<T>(val64, val32, offl + (int64_t)(er - sE0[l]) * Wl + slj - sE0[j] + ec, Kv[k]);
       add_val<T>(val64, val32, offj + (int64_t)(ec - sE0[j]) * Wj + sjl - sE0[l] + er, Kv[k]);
+    }
+  }
+  double* C = nullptr;
+  if constexpr (RHS) {
+    // every read of G.g is done: the hexa's slots may overwrite it
+    __syncthreads();
+    if constexpr (HEXA) C = reinterpret_cast<double*>(&G.g[0][0][0]);
+    else C = S.Cx;
+#pragma unroll
+    for (int q = 0; q < QUU; ++q) {
+      const int pr = threadIdx.x + q * NT;
+      if (pr >= NPAIR) break;
+      int i = int((sqrtf(8.0f * pr + 1.0f) - 1.0f) * 0.5f);
+      while ((i + 1) * (i + 2) / 2 <= pr) ++i;
+      while (i * (i + 1) / 2 > pr) --i;
+      const int j = pr - i * (i + 1) / 2;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        C[(3 * i + k) * NSLOT + j] = ru[q][k];
+        if (i != j) C[(3 * j + k) * NSLOT + i] = ru[q][3 + k];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < QPU; ++q) {
+      const int pr = threadIdx.x + q * NT;
+      if (pr >= NPU) break;
+      const int l = pr / NEN, j = pr % NEN;
+      C[(3 * NEN + l) * NSLOT + j] = rk[q][0];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) C[(3 * j + k) * NSLOT + NEN + l] = rk[q][1 + k];
     }
   }
   // ---- Kpp: vertex pairs (l >= m) ------------------------------------------
@@ -557,6 +640,10 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
       }
     }
     if constexpr (HEXA) acc = imod * am + dtp * ak;
+    if constexpr (RHS) {
+      C[(3 * NEN + l) * NSLOT + NEN + m] = -acc * ul[3 * NEN + m];
+      if (l != m) C[(3 * NEN + m) * NSLOT + NEN + l] = -acc * ul[3 * NEN + l];
+    }
     const int er = sEq[l][3], ec = sEq[m][3];
     if (er == 0 || ec == 0) continue;
     const int nl = E.nodes[l], nm = E.nodes[m];
@@ -567,6 +654,16 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
       add_val<T>(val64, val32,
                  L.node_val_off[nm - 1] + (int64_t)(ec - sE0[m]) * L.node_W[nm - 1] +
                      slot[m * NEN + l] - sE0[l] + er, -acc);
+  }
+  if constexpr (RHS) {
+    __syncthreads();
+    for (int r = threadIdx.x; r < NST; r += NT) {
+      const int e = r < 3 * NEN ? sEq[r / 3][r % 3] : sEq[r - 3 * NEN][3];
+      if (e == 0) continue;
+      double sum = 0;
+      for (int k = 0; k < NSLOT; ++k) sum += C[r * NSLOT + k];
+      bvec[e - 1] -= sum;
+    }
   }
 }
 
@@ -1327,12 +1424,21 @@ __global__ void __launch_bounds__(ET<HEXA>::NT)
 // opt-in above 48 KB set once per kernel.
 template <typename Sm, typename Kern, typename... Args>
 cudaError_t launch_elem(Kern k, int n, int nt, cudaStream_t s, Args... args) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(Sm));
-    if (e != cudaSuccess) return e;
-    attr = true;
+  // kernels of one signature and shared-memory struct (k_assemble_K with and
+  // without the fused product) share this instantiation: key on the kernel
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, int>> opted;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    const std::pair<const void*, int> key(reinterpret_cast<const void*>(k), dev);
+    if (std::find(opted.begin(), opted.end(), key) == opted.end()) {
+      e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
+      if (e != cudaSuccess) return e;
+      opted.push_back(key);
+    }
   }
   k<<<n, nt, sizeof(Sm), s>>>(args...);
   return cudaGetLastError();
@@ -1361,20 +1467,29 @@ cudaError_t ensure_shape_tables() {
 }
 
 cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val64,
-                              float* val32, cudaStream_t s) {
+                              float* val32, cudaStream_t s, const double* u, double* b) {
   if (L.nelem <= 0) return cudaSuccess;
+  const double* nu = nullptr;
+  double* nb = nullptr;
+  if (b && val64) {
+    if (hexa)
+      return launch_elem<SmK<true, double>>(k_assemble_K<true, double, true>, L.nelem, 64, s,
+                                            L, val64, (float*)nullptr, u, b);
+    return launch_elem<SmK<false, double>>(k_assemble_K<false, double, true>, L.nelem, 32, s,
+                                           L, val64, (float*)nullptr, u, b);
+  }
   if (hexa) {
     if (val64)
-      return launch_elem<SmK<true, double>>(k_assemble_K<true, double>, L.nelem, 64, s, L,
-                                            val64, (float*)nullptr);
-    return launch_elem<SmK<true, float>>(k_assemble_K<true, float>, L.nelem, 64, s, L,
-                                         (double*)nullptr, val32);
+      return launch_elem<SmK<true, double>>(k_assemble_K<true, double, false>, L.nelem, 64, s,
+                                            L, val64, (float*)nullptr, nu, nb);
+    return launch_elem<SmK<true, float>>(k_assemble_K<true, float, false>, L.nelem, 64, s, L,
+                                         (double*)nullptr, val32, nu, nb);
   }
   if (val64)
-    return launch_elem<SmK<false, double>>(k_assemble_K<false, double>, L.nelem, 32, s, L,
-                                           val64, (float*)nullptr);
-  return launch_elem<SmK<false, float>>(k_assemble_K<false, float>, L.nelem, 32, s, L,
-                                        (double*)nullptr, val32);
+    return launch_elem<SmK<false, double>>(k_assemble_K<false, double, false>, L.nelem, 32, s,
+                                           L, val64, (float*)nullptr, nu, nb);
+  return launch_elem<SmK<false, float>>(k_assemble_K<false, float, false>, L.nelem, 32, s, L,
+                                        (double*)nullptr, val32, nu, nb);
 }
 
 cudaError_t launch_residual(const ElemLaunch& L, bool hexa, const double* u,
