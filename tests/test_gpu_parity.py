@@ -77,6 +77,25 @@ def test_assembly_matches_oracle(problems):
         assert np.abs(bg - bo).max() <= 1e-11 * max(1.0, np.abs(bo).max())
 
 
+def test_fused_assembly_product_is_deterministic(problems):
+    """pform with lhs and rhs takes b -= K_e u_e from the blocks it assembles:
+    it matches the separate matrix-free pass within rounding, fills the same
+    panels bit for bit, and repeats bit for bit (no atomics in the sums)."""
+    rng = np.random.default_rng(5)
+    for pb in problems:
+        m = pg.from_problem(pb)
+        u = rng.standard_normal((m.nnode, 4)) * 1e-3
+        b0 = rng.standard_normal(m.neq)
+        fused = [m.pform(2, True, True, u, b0.copy()) for _ in range(2)]
+        _, _, ad_f, al_f = m.get_csrd()
+        assert np.array_equal(fused[0], fused[1])
+        m.pform(2, True, False, u, None)
+        _, _, ad_s, al_s = m.get_csrd()
+        sep = m.pform(2, False, True, u, b0.copy())
+        assert np.array_equal(ad_f, ad_s) and np.array_equal(al_f, al_s)
+        assert np.abs(fused[0] - sep).max() <= 1e-12 * max(1.0, np.abs(b0 - sep).max())
+
+
 def test_rhs_isw4_matches_oracle(problems):
     rng = np.random.default_rng(1)
     for pb in problems:
