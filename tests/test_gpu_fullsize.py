@@ -1,0 +1,105 @@
+"""Size-independent properties at the benchmark's full size: the heterogeneous
+hexa20 cube at 56^3 (2,346,120 equations, 3.7 GB of panel values), where the
+oracle cannot run in test time.  The checker is the handle's own CSRD export
+in the reference layout (ia, ja, ad, al) multiplied on the CPU, so the panel
+SpMV, the layout conversion and the solver's stopping test are each checked
+against an independent product."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+sp = pytest.importorskip("scipy.sparse")
+
+import poromec_gb300 as pg  # noqa: E402
+from poromec_gb300 import meshgen  # noqa: E402
+
+N = 56
+
+
+@pytest.fixture(scope="module")
+def cube():
+    pb = meshgen.cube_problem(N)
+    m = pg.from_problem(pb)
+    m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+    ia, ja, ad, al = m.get_csrd()
+    # strictly lower triangle, 1-based CSR rows (Csr.f layout)
+    L = sp.csr_matrix((al, ja.astype(np.int64) - 1, ia - 1), shape=(m.neq, m.neq))
+    absL = sp.csr_matrix((np.abs(al), L.indices, L.indptr), shape=L.shape)
+    yield m, ad, L, absL
+    m.close()
+
+
+def _cpu_spmv(ad, L, x):
+    """matvec_csrc_sym_pm's product y = (D + L + L^T) x, in FP64 on the CPU."""
+    return ad * x + L @ x + L.T @ x
+
+
+def _abs_product(ad, absL, x):
+    ax = np.abs(x)
+    return np.abs(ad) * ax + absL @ ax + absL.T @ ax
+
+
+def test_full_size_spmv_against_the_exported_csrd(cube):
+    m, ad, L, absL = cube
+    assert m.neq == 2346120
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(m.neq)
+    y = m.matvec(x)
+    bound = 1e-13 * _abs_product(ad, absL, x) + 1e-300
+    assert np.all(np.abs(y - _cpu_spmv(ad, L, x)) <= bound)
+
+
+def test_full_size_operator_is_symmetric_and_linear(cube):
+    m, ad, _, absL = cube
+    rng = np.random.default_rng(12)
+    x, y = rng.standard_normal(m.neq), rng.standard_normal(m.neq)
+    ax, ay = m.matvec(x), m.matvec(y)
+    scale = np.abs(y) @ _abs_product(ad, absL, x) + np.abs(x) @ _abs_product(ad, absL, y)
+    assert abs(y @ ax - x @ ay) <= 1e-12 * scale
+    axy = m.matvec(x + 2.0 * y)
+    bound = 1e-13 * (_abs_product(ad, absL, x) + 2.0 * _abs_product(ad, absL, y)) + 1e-300
+    assert np.all(np.abs(axy - (ax + 2.0 * ay)) <= bound)
+
+
+def test_full_size_assembly_repeats_bit_for_bit(cube):
+    m = cube[0]
+    x = np.random.default_rng(13).standard_normal(m.neq)
+    y1 = m.matvec(x)
+    m.pform(2, True, False, np.zeros((m.nnode, 4)), None)
+    assert np.array_equal(m.matvec(x), y1)
+
+
+def test_full_size_compensated_operator_bound(cube):
+    """PM_FP32C_REFINE at full size: each row within 2^-30 (|A| |x|)_i of the
+    FP64 product, the bound the small-case tests check against the oracle."""
+    m, ad, _, absL = cube
+    x = np.random.default_rng(14).standard_normal(m.neq)
+    y64 = m.matvec(x)
+    m.set_precision(pg.capi.PM_FP32C_REFINE)
+    try:
+        yc = m.matvec(x)
+    finally:
+        m.set_precision(pg.capi.PM_FP64)
+    bound = 2.0 ** -30 * _abs_product(ad, absL, x) + 1e-300
+    assert np.all(np.abs(yc - y64) <= bound)
+    assert not np.array_equal(yc, y64)
+
+
+def test_full_size_solve_meets_its_test_on_the_cpu(cube):
+    """pcg's stopping test sqrt|(r, M r)| < tol sqrt|(b, M b)| (Iters.f:434-478),
+    M = 1/ad, re-evaluated with the CPU product of the exported matrix.  pcg
+    stops on its recursive residual; the true one may drift from it over
+    thousands of iterations, hence 1.1 tol rather than tol."""
+    m, ad, L, _ = cube
+    b = np.random.default_rng(15).standard_normal(m.neq)
+    tol = 1e-8
+    x, info = m.solve(b, solver=1, precond=2, tol=tol, maxit=100000)
+    assert info.iters > 0
+    r = b - _cpu_spmv(ad, L, x)
+    rn = np.sqrt(abs(np.sum(r * r / ad)))
+    bn = np.sqrt(abs(np.sum(b * b / ad)))
+    assert rn <= 1.1 * tol * bn, (rn, tol * bn)
