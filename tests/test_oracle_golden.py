@@ -44,19 +44,28 @@ def _run(fx, nsteps):
     return worst, iters
 
 
-@pytest.mark.parametrize("name,nsteps,tol", [
-    ("exemplo1_mesh0_t2", 600, 1e-10),
-    ("exemplo1_mesh0_t2_tetra", 600, 1e-10),
-    ("solo1", 3, 1e-10),
+# (deck, steps, bar, first PCG count equal to the reference's)
+@pytest.mark.parametrize("name,nsteps,tol,first_exact", [
+    ("exemplo1_mesh0_t2", 600, 1e-10, True),
+    ("exemplo1_mesh0_t2_tetra", 600, 1e-10, True),
+    ("solo1", 3, 1e-10, False),
+    # the shipped cylinder decks: element loads read from files, 41 colours for
+    # the tetra.  Their histories sit close to the solver tolerance: rounding
+    # alone moves them by up to ~1e-9 (the hexa deck with this oracle on 1
+    # thread: 9.4e-10; on 8 threads, whose SpMV sums in another order: 5.4e-11)
+    ("solo_cilindro_hexa_1", 5, 2e-9, False),
+    ("solo_cilindro_tetra_1", 5, 2e-9, False),
 ])
-def test_node_histories(golden, name, nsteps, tol):
+def test_node_histories(golden, name, nsteps, tol, first_exact):
     fx = golden(name)
     worst, iters = _run(fx, nsteps)
     # printed with 10 decimals: half a unit of the last digit plus the
     # solver tolerance
     assert worst < tol, worst
     ref_its = fx["pcg_iters"][:nsteps]
-    assert iters[0] == ref_its[0] or name == "solo1"
+    if len(ref_its) == 0:  # the run's log holds no iteration counts
+        return
+    assert iters[0] == ref_its[0] or not first_exact
     # PCG on this indefinite system is sensitive to rounding: the counts agree
     # on average, not step by step
     assert abs(np.mean(iters) - np.mean(ref_its)) <= 0.1 * np.mean(ref_its)
