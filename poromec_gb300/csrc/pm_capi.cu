@@ -173,33 +173,16 @@ int check_elem_err(Handle* h) {
   return PM_OK;
 }
 
-// isw = 2 with lhs: K into the panels (FP64, and FP32 when refining).
-// isw 2 with lhs: the panels; with b also rhs (b -= K_e u_e) in the same
-// element launch.
-int assemble_K(Handle* h, bool fp32, const double* u = nullptr, double* b = nullptr) {
-  if (fp32) {
-    if (!h->P.val32) {
-      PM_CUDA(cudaMalloc(&h->P.val32, sizeof(float) * (size_t)h->P.nnz));
-      if (h->pcgm_graph) {
-        cudaGraphExecDestroy(h->pcgm_graph);
-        h->pcgm_graph = nullptr;
-      }
-    }
-    PM_CUDA(cudaMemsetAsync(h->P.val32, 0, sizeof(float) * (size_t)h->P.nnz, h->stream));
-  } else {
-    PM_CUDA(cudaMemsetAsync(h->P.val, 0, sizeof(double) * (size_t)h->P.nnz, h->stream));
-  }
+// isw 2 with lhs: K into the FP64 panels (the FP32 and compensated copies
+// are rounded from them); with b also rhs (b -= K_e u_e) in the same element
+// launch.
+int assemble_K(Handle* h, const double* u = nullptr, double* b = nullptr) {
+  PM_CUDA(cudaMemsetAsync(h->P.val, 0, sizeof(double) * (size_t)h->P.nnz, h->stream));
   h->launches += h->numcolors;
   for (int c = 0; c < h->numcolors; ++c)
-    PM_CUDA(pm::launch_assemble_K(elem_launch(h, c), h->hexa, fp32 ? nullptr : h->P.val,
-                                  fp32 ? h->P.val32 : nullptr, h->stream, u,
-                                  fp32 ? nullptr : b));
-  if (fp32) {
-    h->assembled32 = true;
-  } else {
-    h->assembled = true;
-    h->assembled32 = h->assembledC = false;
-  }
+    PM_CUDA(pm::launch_assemble_K(elem_launch(h, c), h->hexa, h->P.val, h->stream, u, b));
+  h->assembled = true;
+  h->assembled32 = h->assembledC = false;
   h->assembled_dt = h->dt;
   return PM_OK;
 }
@@ -1351,7 +1334,7 @@ int step_batch(Handle* h, int maxnlit, double tol, int stop_crit, int solver, in
     PM_CUDA(cudaEventRecord(ev[2], s));
     const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
     if (need_K) {
-      PM_TRY(assemble_K(h, false, D.u, D.b));  // b -= K u in the same launch
+      PM_TRY(assemble_K(h, D.u, D.b));  // b -= K u in the same launch
       h->assembled32 = h->assembledC = false;
     } else {
       PM_TRY(residual(h, D.u, D.b));
@@ -1755,9 +1738,9 @@ int pm_assemble(pm_handle hh, int isw, int lhs, int rhs, const double* u, double
                             h->stream));
   if (isw == 2) {
     if (lhs && rhs) {
-      PM_TRY(assemble_K(h, false, h->D.bx, h->D.by));
+      PM_TRY(assemble_K(h, h->D.bx, h->D.by));
     } else if (lhs) {
-      PM_TRY(assemble_K(h, false));
+      PM_TRY(assemble_K(h));
     } else if (rhs) {
       PM_TRY(residual(h, h->D.bx, h->D.by));
     }
@@ -1873,7 +1856,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
     PM_CUDA(cudaEventRecord(ev[2], s));
     const bool need_K = lhs && (reassemble || !h->assembled || h->assembled_dt != h->dt);
     if (need_K) {
-      PM_TRY(assemble_K(h, false, D.u, D.b));  // b -= K u in the same launch
+      PM_TRY(assemble_K(h, D.u, D.b));  // b -= K u in the same launch
       h->assembled32 = h->assembledC = false;
     }
     PM_CUDA(cudaEventRecord(ev[3], s));

@@ -1466,30 +1466,24 @@ cudaError_t ensure_shape_tables() {
   return e;
 }
 
-cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val64,
-                              float* val32, cudaStream_t s, const double* u, double* b) {
+cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val, cudaStream_t s,
+                              const double* u, double* b) {
   if (L.nelem <= 0) return cudaSuccess;
-  const double* nu = nullptr;
-  double* nb = nullptr;
-  if (b && val64) {
+  float* no32 = nullptr;
+  if (b) {
     if (hexa)
       return launch_elem<SmK<true, double>>(k_assemble_K<true, double, true>, L.nelem, 64, s,
-                                            L, val64, (float*)nullptr, u, b);
+                                            L, val, no32, u, b);
     return launch_elem<SmK<false, double>>(k_assemble_K<false, double, true>, L.nelem, 32, s,
-                                           L, val64, (float*)nullptr, u, b);
+                                           L, val, no32, u, b);
   }
-  if (hexa) {
-    if (val64)
-      return launch_elem<SmK<true, double>>(k_assemble_K<true, double, false>, L.nelem, 64, s,
-                                            L, val64, (float*)nullptr, nu, nb);
-    return launch_elem<SmK<true, float>>(k_assemble_K<true, float, false>, L.nelem, 64, s, L,
-                                         (double*)nullptr, val32, nu, nb);
-  }
-  if (val64)
-    return launch_elem<SmK<false, double>>(k_assemble_K<false, double, false>, L.nelem, 32, s,
-                                           L, val64, (float*)nullptr, nu, nb);
-  return launch_elem<SmK<false, float>>(k_assemble_K<false, float, false>, L.nelem, 32, s, L,
-                                        (double*)nullptr, val32, nu, nb);
+  const double* nu = nullptr;
+  double* nb = nullptr;
+  if (hexa)
+    return launch_elem<SmK<true, double>>(k_assemble_K<true, double, false>, L.nelem, 64, s, L,
+                                          val, no32, nu, nb);
+  return launch_elem<SmK<false, double>>(k_assemble_K<false, double, false>, L.nelem, 32, s, L,
+                                         val, no32, nu, nb);
 }
 
 cudaError_t launch_residual(const ElemLaunch& L, bool hexa, const double* u,

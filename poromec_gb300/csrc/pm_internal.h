@@ -98,11 +98,10 @@ struct ElemLaunch {
 // device; called before a handle's first element launch.
 constexpr int kMaxDevices = 64;
 cudaError_t ensure_shape_tables();
-// With b (FP64 panels only) the same launch also does b -= K_e u_e (isw 2
-// with lhs and rhs) from the element blocks it assembles.
-cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val64,
-                              float* val32, cudaStream_t s, const double* u = nullptr,
-                              double* b = nullptr);
+// Element matrices into the FP64 panels; with b the same launch also does
+// b -= K_e u_e (isw 2 with lhs and rhs) from the blocks it assembles.
+cudaError_t launch_assemble_K(const ElemLaunch& L, bool hexa, double* val, cudaStream_t s,
+                              const double* u = nullptr, double* b = nullptr);
 cudaError_t launch_residual(const ElemLaunch& L, bool hexa, const double* u,
                             double* b, cudaStream_t s);
 cudaError_t launch_rhs4(const ElemLaunch& L, bool hexa, const double* u,
