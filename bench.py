@@ -194,8 +194,10 @@ def profile_traffic(nnz_panel, name="spmv_panel_fp64_cube.md"):
 def cpu_step_estimate(pb, iters, elem_sample=600, pcg_sample=4, threads=None):
     import oracle
     threads = threads or os.cpu_count()
+    # the oracle's timing build (-O3, FMA contraction): a release build's speed
     o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]), int(pb["nen"]),
-                      int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"])
+                      int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"],
+                      timing=True)
     o.set_loads(eload=pb["eload"], load=pb["load"], fload=pb["fload"])
     o.set_env(pb["gravity"], float(pb["dt"]))
     o.set_state(u=pb["u0"], u0=pb["u0"])
@@ -223,8 +225,8 @@ def cpu_step_estimate(pb, iters, elem_sample=600, pcg_sample=4, threads=None):
     t_it = (time.perf_counter() - t0) / pcg_sample
     t_step = t4 + t2l + t2r + iters * t_it
     sample = ("element loops isw4/isw2(lhs)/isw2(rhs) on %d of %d elements scaled to the mesh, "
-              "%d PCG iterations scaled to the step's %d; %d threads" % (S, numel, pcg_sample,
-                                                                         iters, threads))
+              "%d PCG iterations scaled to the step's %d; %d threads; oracle built -O3 with "
+              "FMA contraction" % (S, numel, pcg_sample, iters, threads))
     return t_step, dict(t_isw4=t4, t_isw2_lhs=t2l, t_isw2_rhs=t2r, t_pcg_iter=t_it), sample, threads
 
 

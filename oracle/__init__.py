@@ -4,7 +4,8 @@
 (lmn-labest/poroMec mef/src: Elmlib03.f elmt17_pm/elmt15_pm, Elmlib.f shape
 functions, Pform.f pform_pm, Assbly.f csr, Csr.f/Graph.f/Numeq.f CSRD pattern,
 Matvec.f matvec_csrc_sym_pm, Iters.f pcg/pminres, Main.f solv macro).  This
-module builds it with g++ and wraps it with ctypes.  Only tests/,
+module builds it with g++ (a parity build, and a timing build of the same
+source for the CPU baseline) and wraps it with ctypes.  Only tests/,
 ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may import it; the
 GPU library never does.
 """
@@ -17,24 +18,32 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libporomec_oracle.so")
+# the same source built for timing (bench.py's CPU baseline and reference
+# arm): -O3 with FMA contraction, the flags of a release build of the
+# reference on a host whose compiler contracts (GCC does by default on
+# aarch64); results differ from the parity build by rounding only
+LIB_TIMING = os.path.join(BUILD, "libporomec_oracle_o3.so")
 SRC = os.path.join(HERE, "poromec_oracle.cpp")
 PROP = 15
 NFLOAD = 6
 
 
-def build(force=False):
+def build(force=False, timing=False):
     """Compile the oracle: -O2 without FMA contraction, so the arithmetic
-    follows the reference's x86-64 gfortran -O2 build operation for operation."""
+    follows the reference's x86-64 gfortran -O2 build operation for operation.
+    timing=True builds the timing variant instead (-O3, FMA contraction)."""
     os.makedirs(BUILD, exist_ok=True)
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)
-            and os.path.getmtime(LIB) >= os.path.getmtime(SRC.replace(".cpp", ".h"))):
-        return LIB
-    cmd = ["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-           "-std=c++17", "-o", LIB + ".tmp", SRC]
+    out = LIB_TIMING if timing else LIB
+    if (not force and os.path.exists(out)
+            and os.path.getmtime(out) >= os.path.getmtime(SRC)
+            and os.path.getmtime(out) >= os.path.getmtime(SRC.replace(".cpp", ".h"))):
+        return out
+    flags = ["-O3", "-ffp-contract=fast"] if timing else ["-O2", "-ffp-contract=off"]
+    cmd = ["g++"] + flags + ["-fopenmp", "-fPIC", "-shared", "-std=c++17", "-o", out + ".tmp",
+                             SRC]
     subprocess.check_call(cmd)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(out + ".tmp", out)
+    return out
 
 
 class StepInfo(ctypes.Structure):
@@ -43,16 +52,16 @@ class StepInfo(ctypes.Structure):
                 ("res_p", ctypes.c_double)]
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        _lib = ctypes.CDLL(build())
-        _lib.or_element_flops.restype = ctypes.c_double
-        _lib.or_destroy.restype = None
-    return _lib
+def lib(timing=False):
+    if timing not in _libs:
+        L = ctypes.CDLL(build(timing=timing))
+        L.or_element_flops.restype = ctypes.c_double
+        L.or_destroy.restype = None
+        _libs[timing] = L
+    return _libs[timing]
 
 
 def _p(a):
@@ -83,8 +92,9 @@ class Oracle:
     id (nnode, 4) restraint flags, x (nnode, 3), e (numat, 15), u (nnode, 4).
     """
 
-    def __init__(self, nnode, nnodev, numel, nen, nenv, ix, idf, fnno, x, ie, e, num=None):
-        L = lib()
+    def __init__(self, nnode, nnodev, numel, nen, nenv, ix, idf, fnno, x, ie, e, num=None,
+                 timing=False):
+        L = self._L = lib(timing)
         self.nnode, self.numel, self.nen, self.nenv = nnode, numel, nen, nenv
         self._keep = [_i32(ix), _i32(idf), _i32(fnno), _f64(x), _i32(ie), _f64(e)]
         numa = None if num is None else _i32(num)
@@ -103,13 +113,13 @@ class Oracle:
     def __del__(self):
         try:
             if getattr(self, "h", None):
-                lib().or_destroy(self.h)
+                self._L.or_destroy(self.h)
                 self.h = None
         except Exception:
             pass
 
     def set_loads(self, eload=None, eloadp=None, nload=None, f=None, load=None, fload=None):
-        L = lib()
+        L = self._L
         keep = [None if a is None else _i32(a) for a in (eload, eloadp, nload)]
         fa = None if f is None else _f64(f)
         nl = 0 if load is None else len(load)
@@ -121,18 +131,18 @@ class Oracle:
 
     def set_env(self, gravity, dt, t=0.0, istep=0):
         g = _f64(gravity)
-        _check(lib().or_set_env(self.h, _p(g), ctypes.c_double(dt), ctypes.c_double(t), istep),
+        _check(self._L.or_set_env(self.h, _p(g), ctypes.c_double(dt), ctypes.c_double(t), istep),
                "or_set_env")
 
     def set_state(self, u=None, u0=None, dp=None):
         a = [None if v is None else _f64(v) for v in (u, u0, dp)]
-        _check(lib().or_set_state(self.h, _p(a[0]), _p(a[1]), _p(a[2])), "or_set_state")
+        _check(self._L.or_set_state(self.h, _p(a[0]), _p(a[1]), _p(a[2])), "or_set_state")
 
     def get_state(self):
         u = np.zeros((self.nnode, 4))
         u0 = np.zeros((self.nnode, 4))
         dp = np.zeros(self.nnode)
-        _check(lib().or_get_state(self.h, _p(u), _p(u0), _p(dp)), "or_get_state")
+        _check(self._L.or_get_state(self.h, _p(u), _p(u0), _p(dp)), "or_get_state")
         return u, u0, dp
 
     def stress(self):
@@ -140,24 +150,24 @@ class Oracle:
         (nnode, 6) and Darcy flux (nnode, 3) of the current state."""
         tx, txb, txe = np.zeros((self.nnode, 6)), np.zeros((self.nnode, 6)), np.zeros((self.nnode, 6))
         fl = np.zeros((self.nnode, 3))
-        _check(lib().or_stress(self.h, _p(tx), _p(txb), _p(txe), _p(fl)), "or_stress")
+        _check(self._L.or_stress(self.h, _p(tx), _p(txb), _p(txe), _p(fl)), "or_stress")
         return tx, txb, txe, fl
 
     def set_nkrylov(self, k):
-        _check(lib().or_set_nkrylov(self.h, int(k)), "or_set_nkrylov")
+        _check(self._L.or_set_nkrylov(self.h, int(k)), "or_set_nkrylov")
 
     def get_porosity(self):
         poro = np.zeros(self.nnode)
-        _check(lib().or_get_porosity(self.h, _p(poro)), "or_get_porosity")
+        _check(self._L.or_get_porosity(self.h, _p(poro)), "or_get_porosity")
         return poro
 
     def set_porosity(self, poro):
         a = _f64(poro)
-        _check(lib().or_set_porosity(self.h, _p(a)), "or_set_porosity")
+        _check(self._L.or_set_porosity(self.h, _p(a)), "or_set_porosity")
 
     def get_id(self):
         idr = np.zeros((self.nnode, 4), np.int32)
-        _check(lib().or_get_id(self.h, _p(idr)), "or_get_id")
+        _check(self._L.or_get_id(self.h, _p(idr)), "or_get_id")
         return idr
 
     def get_csrd(self):
@@ -165,52 +175,52 @@ class Oracle:
         ja = np.zeros(self.nad, np.int32)
         ad = np.zeros(self.neq)
         al = np.zeros(self.nad)
-        _check(lib().or_get_csrd(self.h, _p(ia), _p(ja), _p(ad), _p(al)), "or_get_csrd")
+        _check(self._L.or_get_csrd(self.h, _p(ia), _p(ja), _p(ad), _p(al)), "or_get_csrd")
         return ia, ja, ad, al
 
     def set_csrd_values(self, ad, al):
         a, b = _f64(ad), _f64(al)
-        _check(lib().or_set_csrd_values(self.h, _p(a), _p(b)), "or_set_csrd_values")
+        _check(self._L.or_set_csrd_values(self.h, _p(a), _p(b)), "or_set_csrd_values")
 
     def element(self, nel, isw, ul, dpl):
         nst = 3 * self.nen + self.nenv
         s = np.zeros((nst, nst))
         p = np.zeros(nst)
         u, d = _f64(ul), _f64(dpl)
-        _check(lib().or_element(self.h, nel, isw, _p(u), _p(d), _p(s), _p(p)), "or_element")
+        _check(self._L.or_element(self.h, nel, isw, _p(u), _p(d), _p(s), _p(p)), "or_element")
         return s.T.copy(), p  # s is column-major in the reference
 
     def pform(self, isw, lhs, rhs, u, b, nthreads=1):
         ua = _f64(u)
         assert b.dtype == np.float64 and b.flags.c_contiguous
-        _check(lib().or_pform(self.h, isw, int(lhs), int(rhs), _p(ua), _p(b), nthreads),
+        _check(self._L.or_pform(self.h, isw, int(lhs), int(rhs), _p(ua), _p(b), nthreads),
                "or_pform")
         return b
 
     def pform_range(self, isw, lhs, rhs, u, b, nthreads, e_begin, e_end):
         ua = _f64(u)
-        _check(lib().or_pform_range(self.h, isw, int(lhs), int(rhs), _p(ua), _p(b), nthreads,
+        _check(self._L.or_pform_range(self.h, isw, int(lhs), int(rhs), _p(ua), _p(b), nthreads,
                                     e_begin, e_end), "or_pform_range")
         return b
 
     def matvec(self, x, nthreads=1):
         xa = _f64(x)
         y = np.zeros(self.neq)
-        _check(lib().or_matvec(self.h, _p(xa), _p(y), nthreads), "or_matvec")
+        _check(self._L.or_matvec(self.h, _p(xa), _p(y), nthreads), "or_matvec")
         return y
 
     def solve(self, b, solver=1, precond=2, tol=1e-11, maxit=50000, nthreads=1):
         ba = _f64(b)
         x = np.zeros(self.neq)
         info = StepInfo()
-        _check(lib().or_solve(self.h, solver, precond, _p(ba), _p(x), ctypes.c_double(tol),
+        _check(self._L.or_solve(self.h, solver, precond, _p(ba), _p(x), ctypes.c_double(tol),
                               maxit, nthreads, ctypes.byref(info)), "or_solve")
         return x, info
 
     def step(self, maxnlit=2, tol=1e-4, stop_crit=2, solver=1, precond=2, solvtol=1e-11,
              maxit=50000, nthreads=1):
         info = StepInfo()
-        _check(lib().or_step(self.h, maxnlit, ctypes.c_double(tol), stop_crit, solver, precond,
+        _check(self._L.or_step(self.h, maxnlit, ctypes.c_double(tol), stop_crit, solver, precond,
                              ctypes.c_double(solvtol), maxit, nthreads, ctypes.byref(info)),
                "or_step")
         return info
