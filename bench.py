@@ -9,20 +9,26 @@ traction ramped to 5 MPa over 10 steps of 100 s; seeded synthetic inputs.
 
 One step = the reference's 'solv' macro (Main.f:876-1123): nodal loads,
 isw 4 element loop, K re-assembled from the elements (isw 2, as the
-reference does every step), residual, diagonal-PCG solve to 1e-8, residual
-check, state update.  `value` is steps/s with the state resident in HBM;
-`e2e` is the same step through the C ABI with the nodal state copied from
-and back to pinned host buffers every step.  `fp32_refine` is the same
-timed steps with the matrix values held as FP32 + an int8 relative
-correction and the compensated FP32 SpMV inside the FP64 refinement loop (PM_FP32C_REFINE),
-with its error against the FP64 steps and against an FP64 solve at 1e-12.
+reference does every step), residual, diagonal-PCG solve, residual check,
+state update, with the reference's nonlinear settings (maxnlit 500,
+tol 1e-4, Main.f:269-273; stop_crit 1) and a PCG tolerance of 1e-10, at
+which the FP64 steps stay within 1e-8 of an FP64 solve to 1e-12 in u and p.
+`value` is steps/s with the state resident in HBM; `e2e` is the same steps
+through the C ABI with the nodal state copied from and back to pinned host
+buffers every step.  `fp32_refine` is the same timed steps with the matrix
+values held as FP32 + an int8 relative correction and the compensated FP32
+SpMV inside the FP64 refinement loop (PM_FP32C_REFINE), with its error
+against the FP64 steps and, over the first --acc-steps steps, against FP64
+solves to 1e-12.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
   python bench.py --spmv-only [--n 32] [--reps 20] [--precision fp64|fp32c]
       (the SpMV alone on an assembled cube: the command the ncu summaries use)
 
 N > 1 runs N independent replicas (one per GPU; a single mesh does not
-shard without the halo exchange of the reference's MPI path).
+shard without the halo exchange of the reference's MPI path); the batched
+leg shards its instances over the ranks.  Without a torchrun environment,
+--gpus N > 1 starts the N local ranks itself.
 """
 import argparse
 import json
@@ -40,15 +46,36 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Biot steps/s at 2M dof: FP64 plain vs FP32+refine at 1e-8 rel; SpMV HBM GB/s"
 
+# PCG iterations per step of the FP64 GPU steps of the 56^3 cube with the
+# default step settings (PCG tol 1e-10, maxnlit 500, stop_crit 1), steps 1..50,
+# as printed in 'pcg_iterations_per_step' by this bench on a GB300.  The
+# reference arm runs before any GPU step and times the CPU's cost of one PCG
+# iteration; it multiplies that by these counts for the steps it stands for.
+# The oracle takes the same iterations as the GPU within rounding (the
+# step-history parity tests hold nlit equal and the solutions within 1e-10).
+MEASURED_PCG_ITERS = {}
 
-def parse():
+
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=56, help="elements per cube edge")
-    ap.add_argument("--solvtol", type=float, default=1e-8)
+    ap.add_argument("--solvtol", type=float, default=1e-10)
+    ap.add_argument("--maxnlit", type=int, default=500,
+                    help="nonlinear iterations per step (the reference's default, Main.f:271)")
+    ap.add_argument("--acc-steps", type=int, default=2,
+                    help="steps over which the FP64 and mixed results are compared with "
+                         "FP64 solves to 1e-12")
+    ap.add_argument("--ref-iters", type=float, default=0.0,
+                    help="reference arm: PCG iterations per step (default: the measured "
+                         "GPU FP64 counts of the same steps)")
+    ap.add_argument("--pcg-sample", type=int, default=20,
+                    help="CPU timing: PCG iterations timed per sample step")
+    ap.add_argument("--iters-only", action="store_true",
+                    help="print the PCG iterations of steps 1..W+K of the FP64 cube only")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
@@ -78,7 +105,7 @@ def parse():
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"],
                     help="operator of --spmv-only and --profile")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_env():
@@ -86,6 +113,28 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def relaunch_ranks(args):
+    """--gpus N > 1 outside torchrun: start N local ranks of this command
+    (one per GPU, rendezvous on 127.0.0.1) and return their exit status."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           "--nproc-per-node", str(args.gpus), "--master-addr", "127.0.0.1",
+           "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def step_kwargs(args, solver=1):
+    """The 'solv' macro settings of every timed step: the reference's
+    nonlinear defaults (maxnlit 500, tol 1e-4; Main.f:269-273) with the
+    stop test of the shipped decks (stop_crit 1), diagonal preconditioner,
+    re-assembly of K every step."""
+    return dict(maxnlit=args.maxnlit, tol=1e-4, stop_crit=1, solver=solver, precond=2,
+                solvtol=args.solvtol, maxit=200000, reassemble=True)
 
 
 def peaks():
@@ -191,66 +240,165 @@ def profile_traffic(nnz_panel, name="spmv_panel_fp64_cube.md"):
 # OpenMP design: coloured element loop, row-partitioned CSRD SpMV) timed on a
 # bounded sample of the same step, on all host cores.
 # --------------------------------------------------------------------------
-def cpu_step_estimate(pb, iters, elem_sample=600, pcg_sample=4, threads=None):
-    import oracle
-    threads = threads or os.cpu_count()
-    # the oracle's timing build (-O3, FMA contraction): a release build's speed
-    o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]), int(pb["nen"]),
-                      int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"],
-                      timing=True)
-    o.set_loads(eload=pb["eload"], load=pb["load"], fload=pb["fload"])
-    o.set_env(pb["gravity"], float(pb["dt"]))
-    o.set_state(u=pb["u0"], u0=pb["u0"])
-    numel = int(pb["numel"])
-    b = np.zeros(o.neq)
-    du = np.zeros((int(pb["nnode"]), 4))
-    S = min(elem_sample, numel)
-    t0 = time.perf_counter()
-    o.pform_range(4, 0, 1, pb["u0"], b, threads, 1, S + 1)
-    t4 = (time.perf_counter() - t0) * numel / S
-    t0 = time.perf_counter()
-    o.pform_range(2, 1, 1, du, b, threads, 1, S + 1)
-    t2l = (time.perf_counter() - t0) * numel / S
-    t0 = time.perf_counter()
-    o.pform_range(2, 0, 1, du, b, threads, 1, S + 1)
-    t2r = (time.perf_counter() - t0) * numel / S
-    # PCG iterations: the cost per iteration does not depend on the values
-    o.set_csrd_values(np.ones(o.neq), np.full(o.nad, 1e-6))
-    rhs = np.ones(o.neq)
-    t0 = time.perf_counter()
-    try:
-        o.solve(rhs, tol=1e-300, maxit=pcg_sample, nthreads=threads)
-    except oracle.OracleError:
-        pass
-    t_it = (time.perf_counter() - t0) / pcg_sample
-    t_step = t4 + t2l + t2r + iters * t_it
-    sample = ("element loops isw4/isw2(lhs)/isw2(rhs) on %d of %d elements scaled to the mesh, "
-              "%d PCG iterations scaled to the step's %d; %d threads; oracle built -O3 with "
-              "FMA contraction" % (S, numel, pcg_sample, iters, threads))
-    return t_step, dict(t_isw4=t4, t_isw2_lhs=t2l, t_isw2_rhs=t2r, t_pcg_iter=t_it), sample, threads
+class CpuStep:
+    """The work of one 'solv' step of the cube on the host cores, timed on the
+    oracle's timing build (-O3, FMA contraction: a release build's speed) with
+    the reference's OpenMP design on `threads` threads.  A step is one isw 4
+    element pass (rhs), one isw 2 pass assembling K with b -= K du, one isw 2
+    residual pass and the PCG solve; every pass covers all elements of the
+    mesh.  PCG iterations are timed on the assembled matrix and the step's
+    right-hand side; their cost does not depend on the iterate, so the solve
+    costs the measured iteration count times the mean iteration time.
+
+    The oracle is built once (its CSRD pattern set-up is not timed)."""
+
+    def __init__(self, pb, threads=None, assemble=False):
+        import oracle
+        self.oracle = oracle
+        self.threads = threads or os.cpu_count()
+        t0 = time.perf_counter()
+        o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]),
+                          int(pb["nen"]), int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"],
+                          pb["x"], pb["ie"], pb["e"], timing=True)
+        o.set_loads(eload=pb["eload"], load=pb["load"], fload=pb["fload"])
+        o.set_env(pb["gravity"], float(pb["dt"]))
+        o.set_state(u=pb["u0"], u0=pb["u0"])
+        self.o, self.u0 = o, pb["u0"]
+        self.numel = int(pb["numel"])
+        self.b = np.zeros(o.neq)
+        self.du = np.zeros((int(pb["nnode"]), 4))
+        if assemble:
+            # K and the right-hand side before any timed sample, so that the
+            # sampled PCG iterations run on the assembled system
+            o.pform(4, False, True, self.u0, self.b, self.threads)
+            o.pform(2, True, True, self.du, self.b, self.threads)
+        self.setup_s = time.perf_counter() - t0
+        self.t_pass = {"isw4": 0.0, "isw2_lhs": 0.0, "isw2_rhs": 0.0}
+        self.elements = {"isw4": 0, "isw2_lhs": 0, "isw2_rhs": 0}
+        self.t_pcg, self.n_pcg = 0.0, 0
+        self.timed_s = 0.0
+
+    def elements_pass(self, e0, e1, record=True):
+        """Elements [e0, e1) (0-based) of the three element passes."""
+        o, th = self.o, self.threads
+        for key, isw, lhs, u in (("isw4", 4, 0, self.u0), ("isw2_lhs", 2, 1, self.du),
+                                 ("isw2_rhs", 2, 0, self.du)):
+            t0 = time.perf_counter()
+            o.pform_range(isw, lhs, 1, u, self.b, th, e0 + 1, e1 + 1)
+            dt = time.perf_counter() - t0
+            if record:
+                self.t_pass[key] += dt
+                self.elements[key] += e1 - e0
+                self.timed_s += dt
+
+    def pcg(self, n, record=True):
+        """n PCG iterations (pcg, Iters.f:299-595) on the handle's matrix."""
+        t0 = time.perf_counter()
+        try:
+            self.o.solve(self.b, tol=1e-300, maxit=n, nthreads=self.threads)
+        except self.oracle.OracleError:
+            pass  # maxit reached: the sample's iterations are done
+        dt = time.perf_counter() - t0
+        if record:
+            self.t_pcg += dt
+            self.n_pcg += n
+            self.timed_s += dt
+
+    def step_seconds(self, iters):
+        """Seconds of one step with `iters` PCG iterations: the element passes
+        scaled from the elements timed (exactly 1 when every element of each
+        pass was timed once) plus iters times the mean iteration time."""
+        t_el = sum(self.t_pass[k] * self.numel / self.elements[k] for k in self.t_pass)
+        return t_el + iters * self.t_pcg / self.n_pcg
+
+    def parts(self, iters):
+        d = {"t_" + k: round(self.t_pass[k] * self.numel / self.elements[k], 4)
+             for k in self.t_pass}
+        d["t_pcg_iter"] = round(self.t_pcg / self.n_pcg, 6)
+        d["t_solve"] = round(iters * self.t_pcg / self.n_pcg, 3)
+        return d
+
+
+def cpu_baseline(pb, iters, pcg_sample):
+    """The GPU arm's cpu_baseline: one full step's element passes (all
+    elements, in the step's order, so the isw 2 pass assembles K) and
+    pcg_sample PCG iterations on that matrix, with the solve scaled to the
+    GPU FP64 steps' measured mean iteration count."""
+    c = CpuStep(pb)
+    c.elements_pass(0, c.numel)
+    c.pcg(pcg_sample)
+    t = c.step_seconds(iters)
+    sample = ("one full step of element passes (isw 4, isw 2 lhs+rhs, isw 2 rhs over all %d "
+              "elements) and %d PCG iterations on the assembled matrix; the solve is the mean "
+              "iteration time x %.1f, the GPU FP64 steps' mean PCG iterations per step; "
+              "%d threads; oracle built -O3 with FMA contraction (%.1f s timed, %.1f s set-up)"
+              % (c.numel, pcg_sample, iters, c.threads, c.timed_s, c.setup_s))
+    return {"value": 1.0 / t, "unit": "steps/s", "cores": c.threads, "kind": "port",
+            "sample": sample, "parts_s": c.parts(iters)}
+
+
+def reference_iters(args):
+    """PCG iterations per step for the reference arm's steps warmup+1 ..
+    warmup+steps: --ref-iters, else the measured GPU FP64 counts."""
+    if args.ref_iters > 0:
+        return float(args.ref_iters), "--ref-iters"
+    key = (args.n, args.solvtol, args.maxnlit)
+    if key not in MEASURED_PCG_ITERS:
+        raise SystemExit("no measured PCG iteration count for the %d^3 cube at tol %g, maxnlit "
+                         "%d: pass --ref-iters" % key)
+    its = MEASURED_PCG_ITERS[key]
+    lo = min(args.warmup, len(its) - 1)
+    win = its[lo:lo + max(args.steps, 1)]
+    return float(np.mean(win)), ("GPU FP64 steps %d..%d of this workload (measured)"
+                                 % (lo + 1, lo + len(win)))
 
 
 def run_reference(args):
+    """The reference arm: the reference algorithm's CPU implementation (the
+    oracle port) on all host cores, rank 0 only.  Each of the W + K steps times
+    args.pcg_sample PCG iterations on the assembled matrix and one K-th slice
+    of each of the three element passes, so the K timed steps time every
+    element of every pass exactly once; the step time is those passes plus
+    the solve at the measured PCG iterations per step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from poromec_gb300 import meshgen
+    iters, iters_src = reference_iters(args)
+    t_run = time.perf_counter()
     pb = meshgen.cube_problem(args.n)
-    iters = int(os.environ.get("PM_REF_ITERS", "0")) or 2500
-    times = []
-    for k in range(args.warmup + args.steps):
-        t_step, parts, sample, threads = cpu_step_estimate(pb, iters, elem_sample=200,
-                                                           pcg_sample=2)
-        if k >= args.warmup:
-            times.append(t_step)
-    v = 1.0 / statistics.mean(times)
+    c = CpuStep(pb, assemble=True)
+    K = max(args.steps, 1)
+    bounds = [c.numel * j // K for j in range(K + 1)]
+    for k in range(args.warmup):
+        # warm-up: the same PCG sample and an element slice, untimed
+        c.pcg(args.pcg_sample, record=False)
+        c.elements_pass(bounds[k % K], bounds[k % K + 1], record=False)
+    for j in range(K):
+        c.elements_pass(bounds[j], bounds[j + 1])
+        c.pcg(args.pcg_sample)
+    t = c.step_seconds(iters)
+    v = 1.0 / t
+    sample = ("each of the %d timed steps: 1/%d of every element pass (isw 4, isw 2 lhs+rhs, "
+              "isw 2 rhs; together each pass over all %d elements once) and %d PCG iterations "
+              "on the assembled matrix; the step's solve = the mean iteration time x %.1f "
+              "PCG iterations (%s); %d threads; oracle built -O3 with FMA contraction"
+              % (K, K, c.numel, args.pcg_sample, iters, iters_src, c.threads))
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s",
            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+           "ms_per_step": 1e3 * t, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "heterogeneous cube, hexa20 %d^3, PCG tol %g" % (
-               args.n, args.solvtol), "pcg_iterations_per_step": iters},
-           "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+           "config": {"workload": "heterogeneous cube, hexa20 %d^3, PCG tol %g, maxnlit %d, "
+                                  "K re-assembled every step" % (args.n, args.solvtol,
+                                                                  args.maxnlit),
+                      "pcg_iterations_per_step": iters},
+           "projected": {"timed_s": round(c.timed_s, 3), "setup_s": round(c.setup_s, 3),
+                         "run_s": round(time.perf_counter() - t_run, 3),
+                         "note": "ms_per_step is the full step projected from the timed "
+                                 "samples: whole element passes plus the PCG iteration time x "
+                                 "the iterations per step"},
+           "parts_s": c.parts(iters),
+           "cpu_baseline": {"value": v, "unit": "steps/s", "cores": c.threads, "kind": "port",
                             "sample": sample},
            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
@@ -320,8 +468,7 @@ def batched_leg(args, steps, warmup):
     m = pg.from_problem(pb)
     m.set_precision(pg.capi.PM_FP32C_REFINE)
     t_setup = time.perf_counter() - t0
-    kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=1, precond=2,
-              solvtol=float(pb["solvtol"]), maxit=200000, reassemble=True)
+    kw = dict(step_kwargs(args), solvtol=float(pb["solvtol"]))
     for _ in range(warmup):
         m.step(**kw)
     torch.cuda.synchronize()
@@ -420,7 +567,8 @@ def tetra_leg(args, steps, warmup):
     """Unstructured tetra10 workload: --tetra-n^3 hex cells on a 2 x 2 x 1 m box
     split in 6 Kuhn tets, interior vertices jittered, two layers, a point
     source, dt 60 s.  Solver: rpsqmr (solver 11, the reference's default) with
-    the diagonal preconditioner to 1e-8; diagonally preconditioned MINRES
+    the diagonal preconditioner, at the cube's PCG tolerance and nonlinear
+    settings; diagonally preconditioned MINRES
     needs 2e4 iterations per step at 4^3 and 4e5 at 8^3 on this problem and
     PCG fails the nonlinear test at 8^3 (the oracle shows the same), so
     rpsqmr stands in for them.  The same steps from the same state in FP64
@@ -432,8 +580,7 @@ def tetra_leg(args, steps, warmup):
     pb = meshgen.tetra_problem(args.tetra_n)
     m = pg.from_problem(pb)
     dt = float(pb["dt"])
-    kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=11, precond=2,
-              solvtol=float(pb.get("solvtol", 1e-8)), maxit=200000, reassemble=True)
+    kw = step_kwargs(args, solver=11)
     for _ in range(warmup):
         m.step(**kw)
     snap = m.get_state()
@@ -507,18 +654,29 @@ def run_gpu(args):
 
     pb = meshgen.cube_problem(args.n)
     m = pg.from_problem(pb)
-    step_kw = dict(maxnlit=2, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=args.solvtol,
-                   maxit=200000, reassemble=True)
+    step_kw = step_kwargs(args)
     if args.profile:
         if args.precision == "fp32c":
             m.set_precision(pg.capi.PM_FP32C_REFINE)
         info = m.step(**step_kw)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_step": True, "pcg_iterations": info.iters,
-                          "kernels": int(m.timers()[7])}), flush=True)
+        print(json.dumps({"profile_step": True, "pcg_iterations": int(m.timers()[4]),
+                          "nlit": info.nlit, "kernels": int(m.timers()[7])}), flush=True)
         return
+    warm_iters = []
     for _ in range(args.warmup):
         m.step(**step_kw)
+        warm_iters.append(int(m.timers()[4]))
+    if args.iters_only:
+        # the PCG iterations of every step 1..W+K (the reference arm's table)
+        for _ in range(args.steps):
+            m.step(**step_kw)
+            warm_iters.append(int(m.timers()[4]))
+        if rank == 0:
+            print(json.dumps({"iters_only": True, "n": args.n, "solvtol": args.solvtol,
+                              "maxnlit": args.maxnlit, "pcg_iterations": warm_iters}),
+                  flush=True)
+        return
     snap = m.get_state()
     t_snap = args.warmup * float(pb["dt"])
 
@@ -527,14 +685,15 @@ def run_gpu(args):
         m.set_state(*snap)
         m.set_env(pb["gravity"], float(pb["dt"]), t_snap, args.warmup)
     barrier()
-    iters = []
+    iters, nlits = [], []
     timers = []
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             info = m.step(**step_kw)
-            iters.append(info.iters)
             timers.append(m.timers())
+            iters.append(int(timers[-1][4]))
+            nlits.append(info.nlit)
         barrier()
         elapsed = time.perf_counter() - t0
     u64, _, _ = m.get_state()
@@ -560,20 +719,28 @@ def run_gpu(args):
     e2e_elapsed = time.perf_counter() - t0
     nbytes = u_h.nbytes + u0_h.nbytes + dp_h.nbytes
 
-    # Accuracy reference: the same steps in FP64 at tolerance 1e-12 (untimed).
+    # Accuracy references (untimed): the first acc steps from the same state
+    # in FP64 with PCG at 1e-12 and at the bench's tolerance.
+    acc = max(1, min(args.acc_steps, args.steps))
     restore()
-    for _ in range(args.steps):
+    for _ in range(acc):
         m.step(**dict(step_kw, solvtol=1e-12))
     u_ref, _, _ = m.get_state()
+    restore()
+    for _ in range(acc):
+        m.step(**step_kw)
+    u64_acc, _, _ = m.get_state()
 
-    def rel_err(a):
-        eu = float(np.abs(a[:, :3] - u_ref[:, :3]).max() / np.abs(u_ref[:, :3]).max())
-        ep = float(np.abs(a[:, 3] - u_ref[:, 3]).max() / np.abs(u_ref[:, 3]).max())
-        return eu, ep
+    def rel_err(a, ref):
+        eu = float(np.abs(a[:, :3] - ref[:, :3]).max() / np.abs(ref[:, :3]).max())
+        ep = float(np.abs(a[:, 3] - ref[:, 3]).max() / np.abs(ref[:, 3]).max())
+        return {"u": eu, "p": ep}
+
+    budget = 2 * max(max(iters), 1)
 
     def mixed_leg(mode, refine=None):
         """The timed steps again from the same state in another precision
-        mode, bounded to twice the FP64 iteration count per step so that a
+        mode, bounded to twice the FP64 iteration count per solve so that a
         stalled refinement is reported instead of waited for."""
         restore()
         m.set_precision(mode)
@@ -581,34 +748,35 @@ def run_gpu(args):
             m.set_refine(refine)
         mi = []
         try:
-            # one untimed step from the same state: the one-off set-up of the
-            # mode (allocation of the compensated copies, the record layout,
-            # the SpMV autotuner, graph capture) stays out of the timed steps,
-            # as the FP64 path's set-up does
-            m.step(**dict(step_kw, maxit=2 * max(iters)))
+            # the first acc steps untimed from the same state: the one-off
+            # set-up of the mode (compensated copies, record layout, SpMV
+            # autotuner, graph capture) stays out of the timed steps, as the
+            # FP64 set-up does, and their result is compared with the FP64
+            # solves to 1e-12
+            for _ in range(acc):
+                m.step(**dict(step_kw, maxit=budget))
+            um_acc, _, _ = m.get_state()
             restore()
             barrier()
             t0 = time.perf_counter()
             for _ in range(args.steps):
-                info = m.step(**dict(step_kw, maxit=2 * max(iters)))
-                mi.append((info.iters, info.refine))
+                info = m.step(**dict(step_kw, maxit=budget))
+                mi.append((int(m.timers()[4]), info.refine, info.nlit))
             barrier()
             t_mixed = time.perf_counter() - t0
             um, _, _ = m.get_state()
-            eu, ep = rel_err(um)
-            du = float(np.abs(um[:, :3] - u64[:, :3]).max() / np.abs(u64[:, :3]).max())
-            dp_ = float(np.abs(um[:, 3] - u64[:, 3]).max() / np.abs(u64[:, 3]).max())
             out = {"value": world * args.steps / t_mixed, "unit": "steps/s",
                    "speedup_vs_fp64": elapsed / t_mixed,
-                   "rel_err_vs_fp64_same_tol": {"u": du, "p": dp_},
-                   "rel_err_vs_fp64_1e-12": {"u": eu, "p": ep},
-                   "pcg_iterations_per_step": [a for a, _ in mi],
-                   "refine_sweeps_per_step": [b for _, b in mi]}
+                   "rel_err_vs_fp64_same_tol": rel_err(um, u64),
+                   "rel_err_vs_fp64_1e-12": dict(rel_err(um_acc, u_ref), steps=acc),
+                   "pcg_iterations_per_step": [a for a, _, _ in mi],
+                   "refine_sweeps_per_step": [b for _, b, _ in mi],
+                   "nlit_per_step": [c for _, _, c in mi]}
         except pg.PMError as ex:
             torch.cuda.synchronize()
             out = {"value": None, "unit": "steps/s", "status": "no convergence",
                    "detail": str(ex), "steps_completed": len(mi),
-                   "iteration_budget_per_step": 2 * max(iters)}
+                   "iteration_budget_per_solve": budget}
         return out
 
     mixed = plain32 = None
@@ -627,7 +795,7 @@ def run_gpu(args):
     if args.fp32_plain:
         plain32 = mixed_leg(pg.capi.PM_FP32_REFINE, 1e-5)
     m.set_precision(pg.capi.PM_FP64)
-    eu64, ep64 = rel_err(u64)
+    fp64_err = dict(rel_err(u64_acc, u_ref), steps=acc)
 
     # SpMV roofline: the dominant kernel timed alone with CUDA events on the
     # stream it is launched on, 50 launches over the assembled matrix
@@ -639,8 +807,18 @@ def run_gpu(args):
     f64_achieved = 2.0 * m.nnz_panel / (spmv_ms * 1e-3) / 1e12
     traffic = profile_traffic(m.nnz_panel)
     tm = np.mean(np.array(timers), 0)
-
+    neq, nad, nnz_panel = m.neq, m.nad, m.nnz_panel
+    # the legs below run on every rank: the batch shards its instances (with
+    # a MAX all-reduce of the time), the tetra box runs as a replica
+    batched = tetra = None
+    if not args.no_batch:
+        m.close()  # the batch needs the memory more than the finished cube
+        batched = batched_leg(args, args.batch_steps, 1)
+    if not args.no_tetra:
+        tetra = tetra_leg(args, 2, 1)
     if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
         return
     out = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
@@ -648,17 +826,19 @@ def run_gpu(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian random fields, structured mesh)",
         "config": {"workload": "heterogeneous cube, hexa20 %d^3, %d equations, nad %d, "
-                               "PCG tol %g, K re-assembled every step" % (
-                                   args.n, m.neq, m.nad, args.solvtol),
-                   "l2": "inputs larger than L2 (panel values %.2f GB)" % (m.nnz_panel * 8e-9),
+                               "PCG tol %g, maxnlit %d, stop_crit 1, K re-assembled every "
+                               "step" % (args.n, neq, nad, args.solvtol, args.maxnlit),
+                   "l2": "inputs larger than L2 (panel values %.2f GB)" % (nnz_panel * 8e-9),
                    "pcg_iterations_per_step": iters,
+                   "nlit_per_step": nlits,
+                   "pcg_iterations_warmup_steps": warm_iters,
                    "phase_ms": {"pload_isw4": tm[0], "assembly_isw2": tm[1],
                                 "residual_isw2": tm[2], "solve": tm[3]},
                    "replicas": world},
         "e2e": {"value": world * args.steps / e2e_elapsed, "unit": "steps/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
         "spmv_gbs": achieved,
-        "fp64_rel_err_vs_1e-12": {"u": eu64, "p": ep64},
+        "fp64_rel_err_vs_1e-12": fp64_err,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
                      "kernel": "k_spmv<double> (node panels)", "launch_ms": spmv_ms,
@@ -666,7 +846,7 @@ def run_gpu(args):
                      # the kernel's actual bound: one DFMA per stored panel value
                      "fp64_pipe": {"achieved_tflops": f64_achieved, "peak_tflops": f64_peak,
                                    "frac": f64_achieved / f64_peak, "peak_source": f64_src,
-                                   "flops": 2.0 * m.nnz_panel}},
+                                   "flops": 2.0 * nnz_panel}},
         "gpu_launches": int(round(args.steps * tm[7])),
         "clocks": clk.summary(),
     }
@@ -674,16 +854,12 @@ def run_gpu(args):
         out["fp32_refine"] = mixed
     if plain32:
         out["fp32_plain_refine"] = plain32
-    if not args.no_batch:
-        m.close()  # the batch needs the memory more than the finished cube
-        out["batched"] = batched_leg(args, args.batch_steps, 1)
-    if not args.no_tetra:
-        out["tetra"] = tetra_leg(args, 2, 1)
+    if batched:
+        out["batched"] = batched
+    if tetra:
+        out["tetra"] = tetra
     if not args.no_cpu:
-        t_step, parts, sample, threads = cpu_step_estimate(pb, int(np.mean(iters)))
-        out["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": threads,
-                               "kind": "port", "sample": sample,
-                               "parts_s": {k: round(v, 4) for k, v in parts.items()}}
+        out["cpu_baseline"] = cpu_baseline(pb, float(np.mean(iters)), args.pcg_sample)
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -691,6 +867,8 @@ def run_gpu(args):
 
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_ranks(args))
     if args.spmv_only:
         run_spmv_only(args)
     elif args.workload == "batched" and args.impl != "reference":

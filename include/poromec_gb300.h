@@ -260,7 +260,9 @@ int pm_adjoint_grad_dev(pm_handle h, const double* d_lam, const double* d_un,
 
 /* Timing of the last pm_step phases in milliseconds (CUDA events):
  * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,
- * [3] solve, [4] unused (0), [5] device time of the last Krylov solve,
+ * [3] solve, [4] Krylov iterations of all the solves of the last single-mesh
+ * pm_step (the step's info->iters counts its last solve only; 0 for a batch),
+ * [5] device time of the last Krylov solve,
  * [6] Krylov iterations of the last solve, [7] kernels launched by the step. */
 int pm_get_timers(pm_handle h, double* t, int n);
 

@@ -1849,6 +1849,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   PM_CUDA(cudaEventRecord(ev[1], s));
   bool lhs = true;
   int it = 1;
+  long tot_iters = 0;
   pm_step_info loc{};
   double t_asm = 0, t_res = 0, t_sol = 0;
   for (;;) {
@@ -1903,6 +1904,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
     PM_TRY(solve_dev(h, solver, precond, D.b, D.xs, solvtol, maxit, &si));
     PM_CUDA(cudaEventRecord(ev[3], s));
     loc.iters = si.iters;
+    tot_iters += si.iters;
     loc.refine = si.refine;
     loc.conv = si.conv;
     loc.xkx = si.xkx;
@@ -1931,6 +1933,7 @@ int pm_step(pm_handle hh, int maxnlit, double tol, int stop_crit, int solver, in
   h->timers[1] = t_asm;
   h->timers[2] = t_res;
   h->timers[3] = t_sol;
+  h->timers[4] = (double)tot_iters;
   h->launches += 1;  // update_res
   h->timers[7] = (double)(h->launches - launches0);
   if (info) *info = loc;
