@@ -5,7 +5,7 @@
  * The reference (lmn-labest/poroMec, Fortran 77/90) has no FFI layer: its
  * "operator API" is the set of subroutines Main.f calls.  Each entry point
  * below replaces one of them and keeps its argument meaning; the Fortran
- * driver binds them with ISO_C_BINDING.
+ * driver binds them with ISO_C_BINDING interfaces.
  *
  * Conventions
  *  - Arrays are the Fortran arrays, column-major, leading dimension first:
@@ -79,6 +79,14 @@ int pm_mesh_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm,
                    const int32_t* fnno, const double* x, int numat,
                    const int32_t* ie, const double* e, const int32_t* num,
                    pm_handle* out);
+
+/* Node order of the 'mesh' macro: reord (Reord.f:1-44, Main.f:585-590), the
+ * reverse Cuthill-McKee permutation of the node graph (genrcm_v1, fnroot_v1,
+ * rcm_v1, Reord.f:45-430) that the reference computes before numbering the
+ * equations when reordf is true, its default (Main.f:255).  ix(nen+1,numel)
+ * as for pm_mesh_create; num(nnode) receives the 1-based node visited i-th,
+ * to be passed as pm_mesh_create's num.  Host computation: no GPU needed. */
+int pm_reord(int nnode, int numel, int nen, const int32_t* ix, int32_t* num);
 
 /* A batch of independent meshes in one handle (the reference runs one mesh
  * per process; this has no single counterpart there).  The arrays are those
@@ -197,7 +205,11 @@ int pm_matvec_csrd_dev(int neq, const int64_t* d_ia, const int32_t* d_ja,
  * device looks up that array's device address, so make it before any stream
  * capture.  Calls share the array and it keeps the last call's contents:
  * two calls that run at the same time on one GPU (two streams, two host
- * threads) race, so serialise them.  stream may be NULL (legacy stream). */
+ * threads) race, so serialise them.  stream may be NULL (legacy stream).
+ * The matrix is scattered into the scratch with atomic adds, so unlike the
+ * rest of the library its results can differ in the last bits from run to
+ * run (within the solve tolerance).  The looked-up address is kept for the
+ * life of the process: do not call it after cudaDeviceReset on that device. */
 #define PM_NOALLOC_MAX_NEQ 262144
 int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* d_ja,
                         const double* d_ad, const double* d_al, const double* d_b,
@@ -287,7 +299,8 @@ int pm_deck_read(const char* path, pm_deck* d);
 const char* pm_deck_error(void);
 void pm_deck_free(pm_deck d);
 /* Scalars by name: nnode nnodev numel numat nen nenv nloads maxt fstress0
- * mk_quad, the settings in force at the first solv (solver precond maxit
+ * mk_quad, reord (1 unless the config block sets it false), the settings in
+ * force at the first solv (solver precond maxit
  * solvtol maxnlit tol stop_crit nkrylov dt gravity_x gravity_y gravity_z),
  * nprint, nops, unknown_macros. */
 int pm_deck_value(pm_deck d, const char* name, double* v);
@@ -297,7 +310,9 @@ int pm_deck_value(pm_deck d, const char* name, double* v);
 int pm_deck_int_array(pm_deck d, const char* name, const int32_t** p, int64_t* n);
 int pm_deck_real_array(pm_deck d, const char* name, const double** p, int64_t* n);
 /* A handle with the deck's mesh, loads, gravity, dt, initial state and
- * initial stress. */
+ * initial stress; the equations are numbered in pm_reord's node order unless
+ * the deck's config block sets reord false (the reference's default is
+ * true, Main.f:255). */
 int pm_deck_create(pm_deck d, pm_handle* h);
 /* Runs the macro program on h (from pm_deck_create): solv steps with the
  * settings in force, pnup / pnsf writing <prefix>_<up|stress|stressE|stressB|

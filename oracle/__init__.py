@@ -226,6 +226,16 @@ class Oracle:
         return info
 
 
+def reord(nnode, numel, nen, ix, afl=True):
+    """reord (Reord.f:1-44): the reverse Cuthill-McKee node permutation,
+    num[i] = the (1-based) node visited i-th; ix is (numel, nen+1)."""
+    num = np.zeros(int(nnode), np.int32)
+    ixa = _i32(ix)
+    _check(lib().or_reord(int(nnode), int(numel), int(nen), _p(ixa), int(bool(afl)), _p(num)),
+           "or_reord")
+    return num
+
+
 def element_flops(nen, isw=2):
     return lib().or_element_flops(nen, isw)
 

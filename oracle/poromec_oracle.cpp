@@ -1450,12 +1450,192 @@ int pminres(or_handle_s* h, const double* m, const double* b, double* x,
   return OR_OK;
 }
 
+// ---- reverse Cuthill-McKee (Reord.f) ---------------------------------------
+// The routines keep the reference's 1-based arrays: xadj(nnode+1) int64 and
+// adjncy of graph_v1, mask, xls, perm; the level structures live in perm.
+
+// rootls_v1 (Reord.f:282-345)
+void rootls(int root, int64_t* xadj, const int32_t* adjncy, int32_t* mask, int& nlvl,
+            int32_t* xls, int32_t* ls) {
+  mask[root] = 0;
+  ls[1] = root;
+  nlvl = 0;
+  int lvlend = 0, ccsize = 1;
+  for (;;) {
+    const int lbegin = lvlend + 1;
+    lvlend = ccsize;
+    nlvl = nlvl + 1;
+    xls[nlvl] = lbegin;
+    for (int i = lbegin; i <= lvlend; ++i) {
+      const int node = ls[i];
+      const int64_t jstrt = xadj[node], jstop = xadj[node + 1] - 1;
+      for (int64_t j = jstrt; j <= jstop; ++j) {
+        const int nbr = adjncy[j];
+        if (mask[nbr] == 0) continue;
+        ccsize = ccsize + 1;
+        ls[ccsize] = nbr;
+        mask[nbr] = 0;
+      }
+    }
+    if (ccsize - lvlend <= 0) break;
+  }
+  xls[nlvl + 1] = lvlend + 1;
+  for (int i = 1; i <= ccsize; ++i) mask[ls[i]] = 1;
+}
+
+// fnroot_v1 (Reord.f:96-164)
+void fnroot(int& root, int64_t* xadj, const int32_t* adjncy, int32_t* mask, int& nlvl,
+            int32_t* xls, int32_t* ls) {
+  rootls(root, xadj, adjncy, mask, nlvl, xls, ls);
+  const int ccsize = xls[nlvl + 1] - 1;
+  if (nlvl == 1 || nlvl == ccsize) return;
+  for (;;) {
+    const int jstrt = xls[nlvl];
+    int mindeg = ccsize;
+    root = ls[jstrt];
+    if (ccsize != jstrt) {
+      for (int j = jstrt; j <= ccsize; ++j) {
+        const int node = ls[j];
+        int ndeg = 0;
+        for (int64_t k = xadj[node]; k <= xadj[node + 1] - 1; ++k)
+          if (mask[adjncy[k]] > 0) ndeg = ndeg + 1;
+        if (ndeg >= mindeg) continue;
+        root = node;
+        mindeg = ndeg;
+      }
+    }
+    int nunlvl = 0;
+    rootls(root, xadj, adjncy, mask, nunlvl, xls, ls);
+    if (nunlvl <= nlvl) return;
+    nlvl = nunlvl;
+    if (nlvl >= ccsize) return;
+  }
+}
+
+// degree_v1 (Reord.f:346-430): xadj's sign marks the nodes already queued
+void degree(int root, int64_t* xadj, const int32_t* adjncy, const int32_t* mask, int32_t* deg,
+            int& ccsize, int32_t* ls) {
+  ls[1] = root;
+  xadj[root] = -xadj[root];
+  int lvlend = 0;
+  ccsize = 1;
+  for (;;) {
+    const int lbegin = lvlend + 1;
+    lvlend = ccsize;
+    for (int i = lbegin; i <= lvlend; ++i) {
+      const int node = ls[i];
+      const int64_t jstrt = -xadj[node];
+      const int64_t jstop = std::llabs(xadj[node + 1]) - 1;
+      int ideg = 0;
+      for (int64_t j = jstrt; j <= jstop; ++j) {
+        const int nbr = adjncy[j];
+        if (mask[nbr] == 0) continue;
+        ideg = ideg + 1;
+        if (xadj[nbr] < 0) continue;
+        xadj[nbr] = -xadj[nbr];
+        ccsize = ccsize + 1;
+        ls[ccsize] = nbr;
+      }
+      deg[node] = ideg;
+    }
+    if (ccsize - lvlend <= 0) break;
+  }
+  for (int i = 1; i <= ccsize; ++i) xadj[ls[i]] = -xadj[ls[i]];
+}
+
+// rcm_v1 (Reord.f:165-281)
+void rcm(int root, int64_t* xadj, const int32_t* adjncy, int32_t* mask, int32_t* perm,
+         int& ccsize, int32_t* deg) {
+  degree(root, xadj, adjncy, mask, deg, ccsize, perm);
+  mask[root] = 0;
+  if (ccsize <= 1) return;
+  int lvlend = 0, lnbr = 1;
+  while (true) {
+    const int lbegin = lvlend + 1;
+    lvlend = lnbr;
+    for (int i = lbegin; i <= lvlend; ++i) {
+      const int node = perm[i];
+      const int fnbr = lnbr + 1;
+      for (int64_t j = xadj[node]; j <= xadj[node + 1] - 1; ++j) {
+        const int nbr = adjncy[j];
+        if (mask[nbr] == 0) continue;
+        lnbr = lnbr + 1;
+        mask[nbr] = 0;
+        perm[lnbr] = nbr;
+      }
+      if (fnbr >= lnbr) continue;
+      // linear insertion by increasing degree
+      int k = fnbr;
+      do {
+        int l = k;
+        k = k + 1;
+        const int nbr = perm[k];
+        while (l >= fnbr && deg[perm[l]] > deg[nbr]) {
+          perm[l + 1] = perm[l];
+          l = l - 1;
+        }
+        perm[l + 1] = nbr;
+      } while (k < lnbr);
+    }
+    if (lnbr <= lvlend) break;
+  }
+  for (int i = 1, l = ccsize; i <= ccsize / 2; ++i, --l) std::swap(perm[l], perm[i]);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // C API
 // ---------------------------------------------------------------------------
 extern "C" {
+
+// reord (Reord.f:1-44) with graph_v1 (Graph.f:72-133) and genrcm_v1
+// (Reord.f:45-95); afl = 0 gives the identity.
+int or_reord(int nnode, int numel, int nen, const int32_t* ix, int afl, int32_t* iperm) {
+  if (nnode < 1 || numel < 0 || nen < 1 || !iperm || (numel > 0 && !ix)) return OR_E_ARG;
+  if (!afl) {
+    for (int i = 0; i < nnode; ++i) iperm[i] = i + 1;
+    return OR_OK;
+  }
+  // graph_v1: every node of an element is a neighbour of the others, lists
+  // sorted by node number without repeats (1-based xadj / adjncy)
+  std::vector<std::vector<int32_t>> nb(nnode + 1);
+  for (int el = 0; el < numel; ++el) {
+    const int32_t* nodes = ix + (size_t)(nen + 1) * el;
+    for (int j = 0; j < nen; ++j) {
+      const int noj = nodes[j];
+      if (noj == 0 || noj > nnode) continue;
+      for (int k = 0; k < nen; ++k) {
+        const int nok = nodes[k];
+        if (nok == 0 || nok > nnode || nok == noj) continue;
+        nb[noj].push_back(nok);
+      }
+    }
+  }
+  std::vector<int64_t> xadj(nnode + 2, 0);
+  xadj[1] = 1;
+  for (int n = 1; n <= nnode; ++n) {
+    std::sort(nb[n].begin(), nb[n].end());
+    nb[n].erase(std::unique(nb[n].begin(), nb[n].end()), nb[n].end());
+    xadj[n + 1] = xadj[n] + (int64_t)nb[n].size();
+  }
+  std::vector<int32_t> adjncy(xadj[nnode + 1] + 1, 0);
+  for (int n = 1; n <= nnode; ++n)
+    std::copy(nb[n].begin(), nb[n].end(), adjncy.begin() + xadj[n]);
+  // genrcm_v1
+  std::vector<int32_t> perm(nnode + 2, 0), mask(nnode + 1, 1), xls(nnode + 2, 0);
+  int num = 1;
+  for (int i = 1; i <= nnode; ++i) {
+    if (mask[i] == 0) continue;
+    int root = i, nlvl = 0, ccsize = 0;
+    fnroot(root, xadj.data(), adjncy.data(), mask.data(), nlvl, xls.data(), perm.data() + num - 1);
+    rcm(root, xadj.data(), adjncy.data(), mask.data(), perm.data() + num - 1, ccsize, xls.data());
+    num = num + ccsize;
+    if (num > nnode) break;
+  }
+  for (int i = 1; i <= nnode; ++i) iperm[i - 1] = perm[i];
+  return OR_OK;
+}
 
 static void initial_porosity(or_handle_s* h);
 

@@ -48,6 +48,12 @@ enum { OR_OK = 0, OR_E_ARG = 1, OR_E_DET = 2, OR_E_ZERO_DIAG = 3,
  * id is the restraint flag array as read by constrainpmec (1 = prescribed).
  * num: node permutation (1-based, num(i) = i-th node visited), or NULL for
  * identity (reord false). */
+/* reord (Reord.f:1-44): reverse Cuthill-McKee permutation of the node graph
+ * of graph_v1 (Graph.f:72-133) by genrcm_v1 / fnroot_v1 / rcm_v1 /
+ * rootls_v1 / degree_v1 (Reord.f:45-430); iperm(i) is the node visited
+ * i-th (1-based), the num argument of or_create.  afl = 0: identity. */
+int or_reord(int nnode, int numel, int nen, const int32_t* ix, int afl, int32_t* iperm);
+
 int or_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndf,
               const int32_t* ix, const int32_t* id, const int32_t* fnno,
               const double* x, int numat, const int32_t* ie, const double* e,

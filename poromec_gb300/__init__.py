@@ -6,6 +6,6 @@ the reference's element/solver call surface, :mod:`poromec_gb300.meshgen`
 builds the seeded benchmark problems.
 """
 from . import meshgen  # noqa: F401
-from .capi import Mesh, PMError, StepInfo, from_problem, load, matvec_csrd_dev  # noqa: F401
+from .capi import Mesh, PMError, StepInfo, from_problem, load, matvec_csrd_dev, reord  # noqa: F401
 
 __all__ = ["Mesh", "PMError", "StepInfo", "from_problem", "load", "matvec_csrd_dev", "meshgen"]

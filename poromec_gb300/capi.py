@@ -26,7 +26,8 @@ PM_FP32C_REFINE = 2
 STATUS = {0: "ok", 1: "invalid argument", 2: "element Jacobian determinant <= 1e-14",
           3: "zero diagonal coefficient", 4: "Krylov solver did not converge",
           5: "nonlinear iteration did not converge", 6: "unsupported element type",
-          7: "CUDA error", 8: "device allocation failed", 9: "call out of order"}
+          7: "CUDA error", 8: "device allocation failed", 9: "call out of order",
+          10: "problem larger than the fixed scratch of pm_pcg_csrd_noalloc"}
 
 
 class PMError(RuntimeError):
@@ -64,6 +65,7 @@ def load(path=None):
     lib.pm_destroy.restype = None
     lib.pm_destroy.argtypes = [c_p]
     lib.pm_mesh_create.argtypes = [c_i] * 7 + [c_p] * 4 + [c_i] + [c_p] * 4
+    lib.pm_reord.argtypes = [c_i, c_i, c_i, c_p, c_p]
     lib.pm_batch_create.argtypes = [c_i] * 7 + [c_p] * 4 + [c_i] + [c_p] * 2 + [c_i] + [c_p] * 2
     lib.pm_get_batch_iters.argtypes = [c_p, c_p, c_p, c_i]
     lib.pm_set_loads.argtypes = [c_p] * 5 + [c_i, c_i, c_p, c_p]
@@ -381,10 +383,25 @@ def matvec_csrd_dev(neq, ia_ptr, ja_ptr, ad_ptr, al_ptr, x_ptr, y_ptr, stream=No
         raise PMError(st, "pm_matvec_csrd_dev")
 
 
-def from_problem(pb, num=None):
+def reord(nnode, numel, nen, ix):
+    """reord (Reord.f:1-44): the reference's reverse Cuthill-McKee node
+    order; num[i] is the 1-based node visited i-th (pm_mesh_create's num).
+    ix is (numel, nen+1)."""
+    num = np.zeros(int(nnode), np.int32)
+    ixa = _i32(ix)
+    st = load().pm_reord(int(nnode), int(numel), int(nen), _p(ixa), _p(num))
+    if st != 0:
+        raise PMError(st, "pm_reord")
+    return num
+
+
+def from_problem(pb, num=None, rcm=False):
     """Mesh for a problem dict (the keys of tests/golden fixtures and of
     poromec_gb300.meshgen problems) with loads, gravity, dt and the initial
-    state applied."""
+    state applied.  rcm=True numbers the equations in the reference's
+    reverse Cuthill-McKee node order (reord true) unless num is given."""
+    if num is None and rcm:
+        num = reord(pb["nnode"], pb["numel"], pb["nen"], pb["ix"])
     m = Mesh(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]), int(pb["nen"]),
              int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"], pb["x"], pb["ie"], pb["e"],
              num=num, inst_node_ptr=pb.get("inst_node_ptr"))

@@ -81,6 +81,13 @@ bool to_int(const std::string& t, long* v) {
   return end && *end == '\0' && !t.empty();
 }
 
+// Fortran list-directed logical: an optional '.', then T or F (any case)
+// decides; the rest of the word is ignored ("true", ".false.", "T").
+bool fortran_logical(const std::string& t) {
+  const size_t k = (!t.empty() && t[0] == '.') ? 1 : 0;
+  return k < t.size() && (t[k] == 't' || t[k] == 'T');
+}
+
 std::vector<std::string> split(const std::string& line) {
   std::vector<std::string> w;
   std::string cur;
@@ -178,6 +185,7 @@ struct pm_deck_s {
   std::string path, dir;
   int nnode = 0, nnodev = 0, numel = 0, numat = 0, nen = 0, nenv = 0, ndf = 0, ndm = 0;
   bool elements_read = false, mk_quad = false, fstress0 = false, mesh_done = false;
+  bool reord = true;  // reordf (Main.f:255): RCM node order unless config says false
   std::vector<int32_t> ix, ie, id, nload, eload, eloadp, fnno, load, print_nodes;
   std::vector<double> e, x, f, u0, tx0, fload;
   int nloads = 0, maxt = 1;
@@ -767,8 +775,19 @@ bool parse(Reader& r, pm_deck_s* d) {
       if (!read_mesh(r, d, s)) return false;
       d->init = s;
     } else if (m == "config") {
-      while (r.next(w) && w[0] != "end") {
+      // read_config (Rdata.f:2929-3110): "key value" pairs up to 'end', inline
+      // in the older decks, in a named file in the current syntax; only
+      // reord changes what the library computes (RCM node order, on by
+      // default as reordf in Main.f:255)
+      Reader cf;
+      Reader* src = &r;
+      if (w.size() >= 2) {
+        if (!cf.push(join(d->dir, w[1]))) return fail(r, cf.err);
+        src = &cf;
       }
+      while (src->next(w) && w[0] != "end")
+        for (size_t k = 0; k + 1 < w.size(); k += 2)
+          if (w[k] == "reord") d->reord = fortran_logical(w[k + 1]);
     } else if (m == "pcg") {  // older decks: "pcg maxit tol"
       long it;
       double tol;
@@ -1219,7 +1238,8 @@ int pm_deck_value(pm_deck d, const char* name, double* v) {
   const std::map<std::string, double> vals = {
       {"nnode", d->nnode}, {"nnodev", d->nnodev}, {"numel", d->numel}, {"numat", d->numat},
       {"nen", d->nen}, {"nenv", d->nenv}, {"nloads", d->nloads}, {"maxt", d->maxt},
-      {"fstress0", d->fstress0}, {"mk_quad", d->mk_quad}, {"solver", s.solver},
+      {"fstress0", d->fstress0}, {"mk_quad", d->mk_quad}, {"reord", d->reord},
+      {"solver", s.solver},
       {"precond", s.precond}, {"maxit", s.maxit}, {"solvtol", s.solvtol},
       {"maxnlit", s.maxnlit}, {"tol", s.tol}, {"stop_crit", s.stop_crit},
       {"nkrylov", s.nkrylov}, {"dt", s.dt}, {"gravity_x", s.gravity[0]},
@@ -1259,9 +1279,16 @@ int pm_deck_real_array(pm_deck d, const char* name, const double** p, int64_t* n
 
 int pm_deck_create(pm_deck d, pm_handle* h) {
   if (!d || !h) return PM_E_ARG;
+  // the mesh macro numbers the equations in reord's node order (Main.f:585-590)
+  std::vector<int32_t> num;
+  if (d->reord) {
+    num.resize(d->nnode);
+    int st = pm_reord(d->nnode, d->numel, d->nen, d->ix.data(), num.data());
+    if (st != PM_OK) return st;
+  }
   int st = pm_mesh_create(d->nnode, d->nnodev, d->numel, d->nen, d->nenv, 3, kNdf, d->ix.data(),
                           d->id.data(), d->fnno.data(), d->x.data(), d->numat, d->ie.data(),
-                          d->e.data(), nullptr, h);
+                          d->e.data(), d->reord ? num.data() : nullptr, h);
   if (st != PM_OK) return st;
   std::vector<double> zero(d->nnode, 0.0);
   if ((st = pm_set_loads(*h, d->eload.data(), d->eloadp.data(), d->nload.data(), d->f.data(),

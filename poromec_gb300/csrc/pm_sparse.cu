@@ -1931,6 +1931,10 @@ extern "C" int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* 
   if (neq > kNoAllocMaxNeq) return PM_E_TOO_LARGE;
   if (neq <= 0 || !d_ia || !d_ja || !d_ad || !d_al || !d_b || !d_x || maxit < 1 || !(tol >= 0.0))
     return PM_E_ARG;
+  // an error left by the caller's earlier launches is theirs: report it
+  // before launching anything (without clearing it), so that errors of this
+  // solve are not confused with it
+  if (cudaPeekAtLastError() != cudaSuccess) return PM_E_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices)
     return PM_E_CUDA;
@@ -1964,6 +1968,7 @@ extern "C" int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* 
   k_precond<<<g, 256, 0, s>>>(neq, d_ad, m, 0, zero_diag);
   k_pcg_init<<<g, 256, 0, s>>>(neq, d_b, m, V.r, V.z, V.p, V.x, ks, tol, maxit, partial,
                                 counter);
+  if (cudaGetLastError() != cudaSuccess) return PM_E_CUDA;
   int zd = 0;
   if (cudaMemcpyAsync(&zd, zero_diag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
@@ -1989,6 +1994,3 @@ extern "C" int pm_pcg_csrd_noalloc(int neq, const int64_t* d_ia, const int32_t* 
   if (iters) *iters = h.iter;
   return h.conv_flag == 1 ? PM_OK : PM_E_NOCONV;
 }
-
-namespace pm {
-}  // namespace pm

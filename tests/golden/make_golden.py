@@ -13,7 +13,8 @@ holding the mesh arrays, loads, initial state, solver settings and the expected
 outputs.  The fixtures are what the tests read; nothing at test time touches
 the reference tree.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
+        (or with the environment variable POROMEC_REFERENCE set to it)
 """
 import os
 import re
@@ -307,7 +308,10 @@ def check_library_reader(ref_root, kind, deck, prefix):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("POROMEC_REFERENCE")
+    if not ref_root:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT (or set POROMEC_REFERENCE): "
+                         "the root of a poroMec checkout holding output/poro_mec/elastico")
     for kind, deck, prefix in CASES:
         name, counts, nnode = convert(ref_root, kind, deck, prefix)
         checked = False

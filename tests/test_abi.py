@@ -34,6 +34,18 @@ def test_status_strings_without_gpu():
     assert b"converge" in lib.pm_status_string(4)
 
 
+def test_python_status_table_matches_the_library():
+    """capi.STATUS gives every status code the library's own text."""
+    from poromec_gb300 import capi
+    lib = ctypes.CDLL(gbuild.build())
+    lib.pm_status_string.restype = ctypes.c_char_p
+    src = open(os.path.join(ROOT, "include", "poromec_gb300.h")).read()
+    codes = sorted(int(v) for v in re.findall(r"PM_(?:OK|E_[A-Z_]+)\s*=\s*(\d+)", src))
+    assert codes == list(range(len(codes))) and len(codes) >= 11
+    for c in codes:
+        assert capi.STATUS[c] == lib.pm_status_string(c).decode(), c
+
+
 def test_create_rejects_bad_arguments_without_touching_the_gpu():
     lib = ctypes.CDLL(gbuild.build())
     h = ctypes.c_void_p()

@@ -5,9 +5,14 @@ Each instance runs its own PCG (own scalars, stopping test and nonlinear
 test); only the launches are shared.  The per-instance dot products are
 summed in a different order than a single handle's, so iteration counts
 may differ by rounding; solutions agree within the solver tolerance times
-the conditioning (the bars below)."""
+the conditioning (the bars below).  The batch is also checked against the
+oracle stepping each instance alone (the reference's algorithm on the CPU)."""
+import os
+
 import numpy as np
 import pytest
+
+import oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -81,6 +86,43 @@ def test_batch_steps_match_single(instances, precision):
         for sl in (slice(0, 3), slice(3, 4)):
             ref = us[:, sl]
             assert np.abs(part[:, sl] - ref).max() <= 1e-8 * np.abs(ref).max(), (k, sl)
+
+
+@pytest.mark.parametrize("precision,bar", [(pg.capi.PM_FP64, 1e-10),
+                                           (pg.capi.PM_FP32C_REFINE, 1e-8)])
+def test_batch_steps_match_oracle(precision, bar):
+    """Eight instances of uneven size (edges 2..6, own E and k) stepped three
+    times in one handle, against the oracle stepping each instance alone:
+    every instance stops at the oracle's nonlinear iteration, and u and p
+    agree within 1e-10 (FP64) or 1e-8 (compensated operator in FP64
+    refinement) of their largest value.  PCG runs to 1e-13, where the solver
+    resolves these bars."""
+    inst = meshgen.batch_instances(ninst=8, nmin=2, nmax=6, seed=23)
+    assert len({p["n"] for p in inst}) > 2
+    pb = meshgen.union_problem(inst)
+    mb = pg.from_problem(pb)
+    mb.set_precision(precision)
+    kw = dict(maxnlit=500, tol=1e-4, stop_crit=1, precond=2, solvtol=1e-13, maxit=200000)
+    orcs = []
+    for p in inst:
+        o = oracle.Oracle(int(p["nnode"]), int(p["nnodev"]), int(p["numel"]), int(p["nen"]),
+                          int(p["nenv"]), p["ix"], p["id"], p["fnno"], p["x"], p["ie"], p["e"])
+        o.set_loads(eload=p["eload"], load=p["load"], fload=p["fload"])
+        o.set_env(p["gravity"], float(p["dt"]))
+        o.set_state(u=p["u0"], u0=p["u0"])
+        orcs.append(o)
+    for step in range(3):
+        mb.step(solver=1, **kw)
+        _, nl = mb.batch_iters()
+        for k, o in enumerate(orcs):
+            info = o.step(solver=1, nthreads=os.cpu_count(), **kw)
+            assert nl[k] == info.nlit, (step, k, nl[k], info.nlit)
+    ub, _, _ = mb.get_state()
+    for k, (o, part) in enumerate(zip(orcs, _split(ub, pb["inst_node_ptr"]))):
+        uo, _, _ = o.get_state()
+        for sl in (slice(0, 3), slice(3, 4)):
+            ref = uo[:, sl]
+            assert np.abs(part[:, sl] - ref).max() <= bar * np.abs(ref).max(), (k, sl)
 
 
 def test_batch_rejects_minres(instances):

@@ -277,6 +277,50 @@ def test_golden_histories_on_gpu(golden, name):
     assert worst < 1e-10, worst
 
 
+def test_rcm_numbering_pattern_and_values_match_oracle(problems):
+    """reord true (the reference's default): with the node order of pm_reord
+    (host) and of the oracle's or_reord, the equation numbers and the CSRD
+    pattern are equal bit for bit, the assembled values within the assembly
+    bar, and the order differs from the natural one."""
+    rng = np.random.default_rng(4)
+    for pb in problems:
+        num = pg.reord(pb["nnode"], pb["numel"], pb["nen"], pb["ix"])
+        num_o = oracle.reord(pb["nnode"], pb["numel"], pb["nen"], pb["ix"])
+        assert np.array_equal(num, num_o)
+        m = pg.from_problem(pb, num=num)
+        o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]),
+                          int(pb["nen"]), int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"],
+                          pb["x"], pb["ie"], pb["e"], num=num_o)
+        assert m.neq == o.neq and m.nad == o.nad
+        assert np.array_equal(m.get_id(), o.get_id())
+        du = rng.standard_normal((m.nnode, 4)) * 1e-3
+        bg, bo = np.zeros(m.neq), np.zeros(m.neq)
+        m.pform(2, True, True, du, bg)
+        o.pform(2, True, True, du, bo)
+        ia, ja, ad, al = m.get_csrd()
+        iao, jao, ado, alo = o.get_csrd()
+        assert np.array_equal(ia, iao) and np.array_equal(ja, jao)
+        scale = max(np.abs(ado).max(), np.abs(alo).max())
+        assert np.abs(ad - ado).max() <= 1e-12 * scale
+        assert np.abs(al - alo).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_histories_with_rcm_order(golden, name):
+    """The golden Terzaghi columns rerun with the equations in RCM order
+    (their decks say reord false): the 600-step node histories still match
+    the reference's printed values within 1e-10."""
+    fx = golden(name)
+    m = pg.from_problem(fx, rcm=True)
+    worst = 0.0
+    for k in range(1, 601):
+        m.step(maxnlit=2, stop_crit=1, solvtol=float(fx["solver_tol"]), maxit=int(fx["maxit"]))
+        u, _, _ = m.get_state()
+        for a, n in enumerate(fx["hist_nodes"]):
+            worst = max(worst, np.abs(u[n - 1] - fx["hist"][a][k][2:6]).max())
+    assert worst < 1e-10, worst
+
+
 def test_column_steps_match_oracle():
     pb = meshgen.column_problem()
     m, o = _pair(pb)
