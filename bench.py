@@ -108,6 +108,17 @@ def parse(argv=None):
     return ap.parse_args(argv)
 
 
+T_START = time.perf_counter()
+
+
+def log(msg):
+    """Progress on stderr (rank 0): seconds since start and what just ended,
+    so that a run cut short still shows where its time went."""
+    if int(os.environ.get("RANK", "0")) == 0:
+        print("[bench %7.1f s] %s" % (time.perf_counter() - T_START, msg), file=sys.stderr,
+              flush=True)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -469,8 +480,10 @@ def batched_leg(args, steps, warmup):
     m.set_precision(pg.capi.PM_FP32C_REFINE)
     t_setup = time.perf_counter() - t0
     kw = dict(step_kwargs(args), solvtol=float(pb["solvtol"]))
+    log("batch set up: %d instances, %d equations (%.1f s)" % (len(inst), m.neq, t_setup))
     for _ in range(warmup):
         m.step(**kw)
+        log("batch warm-up step: max PCG iterations %d" % m.batch_iters()[0].max())
     torch.cuda.synchronize()
     its = []
     t0 = time.perf_counter()
@@ -581,8 +594,10 @@ def tetra_leg(args, steps, warmup):
     m = pg.from_problem(pb)
     dt = float(pb["dt"])
     kw = step_kwargs(args, solver=11)
+    log("tetra set up: %d equations" % m.neq)
     for _ in range(warmup):
         m.step(**kw)
+        log("tetra warm-up step: %d iterations" % int(m.timers()[4]))
     snap = m.get_state()
 
     def restore():
@@ -594,7 +609,9 @@ def tetra_leg(args, steps, warmup):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(steps):
-            its.append(m.step(**kw).iters)
+            m.step(**kw)
+            its.append(int(m.timers()[4]))
+            log("tetra step: %d iterations" % its[-1])
         torch.cuda.synchronize()
         return time.perf_counter() - t0, its
 
@@ -654,6 +671,7 @@ def run_gpu(args):
 
     pb = meshgen.cube_problem(args.n)
     m = pg.from_problem(pb)
+    log("cube %d^3 set up: %d equations" % (args.n, m.neq))
     step_kw = step_kwargs(args)
     if args.profile:
         if args.precision == "fp32c":
@@ -665,8 +683,10 @@ def run_gpu(args):
         return
     warm_iters = []
     for _ in range(args.warmup):
-        m.step(**step_kw)
+        info = m.step(**step_kw)
         warm_iters.append(int(m.timers()[4]))
+        log("warm-up step %d: %d PCG iterations, nlit %d" % (len(warm_iters), warm_iters[-1],
+                                                             info.nlit))
     if args.iters_only:
         # the PCG iterations of every step 1..W+K (the reference arm's table)
         for _ in range(args.steps):
@@ -694,8 +714,10 @@ def run_gpu(args):
             timers.append(m.timers())
             iters.append(int(timers[-1][4]))
             nlits.append(info.nlit)
+            log("timed step %d: %d PCG iterations, nlit %d" % (len(iters), iters[-1], info.nlit))
         barrier()
         elapsed = time.perf_counter() - t0
+    log("timed FP64 steps: %.2f s/step" % (elapsed / args.steps))
     u64, _, _ = m.get_state()
     ms = elapsed / args.steps * 1e3
     if world > 1:
@@ -718,6 +740,7 @@ def run_gpu(args):
     barrier()
     e2e_elapsed = time.perf_counter() - t0
     nbytes = u_h.nbytes + u0_h.nbytes + dp_h.nbytes
+    log("e2e steps: %.2f s/step" % (e2e_elapsed / args.steps))
 
     # Accuracy references (untimed): the first acc steps from the same state
     # in FP64 with PCG at 1e-12 and at the bench's tolerance.
@@ -730,6 +753,7 @@ def run_gpu(args):
     for _ in range(acc):
         m.step(**step_kw)
     u64_acc, _, _ = m.get_state()
+    log("accuracy references (%d steps at 1e-12 and at the bench tolerance)" % acc)
 
     def rel_err(a, ref):
         eu = float(np.abs(a[:, :3] - ref[:, :3]).max() / np.abs(ref[:, :3]).max())
@@ -782,6 +806,7 @@ def run_gpu(args):
     mixed = plain32 = None
     if not args.no_mixed:
         mixed = mixed_leg(pg.capi.PM_FP32C_REFINE)
+        log("compensated steps: %s steps/s" % mixed.get("value"))
         # the compensated SpMV alone (x split into its FP32 pair included)
         cms = time_spmv(m, torch, 50)
         cB = spmv_bytes(m.nad, m.neq, comp=True)
@@ -814,8 +839,10 @@ def run_gpu(args):
     if not args.no_batch:
         m.close()  # the batch needs the memory more than the finished cube
         batched = batched_leg(args, args.batch_steps, 1)
+        log("batched leg: %.2f instance-steps/s" % batched["value"])
     if not args.no_tetra:
         tetra = tetra_leg(args, 2, 1)
+        log("tetra leg: %.3f steps/s" % tetra["value"])
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -860,6 +887,7 @@ def run_gpu(args):
         out["tetra"] = tetra
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(pb, float(np.mean(iters)), args.pcg_sample)
+        log("cpu baseline: %.5f steps/s" % out["cpu_baseline"]["value"])
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
