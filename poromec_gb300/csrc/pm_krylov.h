@@ -207,6 +207,11 @@ cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,
 cudaError_t pcgc_iteration(const PanelView& P, CompVals C, int n, const double* m,
                            KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
                            double* partial, unsigned* counter, cudaStream_t s);
+// residual replacement of the compensated PCG: r = b - q (q = A x in FP64),
+// z = m r, d = (r, z), flags re-decided; x and p kept
+cudaError_t pcgc_replace(int n, const double* b, const double* q, const double* m,
+                         KrylovVecs& V, KrylovScalars* ks, double* partial, unsigned* counter,
+                         cudaStream_t s);
 cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const double* m,
                               KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
                               double* partial, unsigned* counter, cudaStream_t s);

@@ -1203,6 +1203,40 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Residual replacement in the PCG on the compensated operator (van der Vorst
+// and Ye, "Residual replacement strategies for Krylov subspace iterative
+// methods for the convergence of true residuals", SIAM J. Sci. Comput. 22,
+// 2000): the recursive residual, updated with the compensated products,
+// drifts from b - A x by the operator's error times the change of x; it is
+// replaced by r = b - q (q = A x by the FP64 operator), z = m r,
+// d = (r, z), while x and the search direction p are kept, so the Krylov
+// iteration goes on instead of restarting.  The flags are re-decided from
+// the replaced residual: converged only when it meets pcg's test.
+__global__ void __launch_bounds__(256)
+    k_pcgc_replace(int n, const double* __restrict__ b, const double* __restrict__ q,
+                   const double* __restrict__ m, double* __restrict__ r,
+                   double* __restrict__ z, KrylovScalars* ks, double* partial,
+                   unsigned* counter) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double ri = b[i] - q[i];
+    const double zi = ri * m[i];
+    r[i] = ri;
+    z[i] = zi;
+    acc += ri * zi;
+  }
+  double in[1] = {acc}, tot[1];
+  if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
+    const double di = tot[0];
+    ks->d = di;
+    ks->done = 0;
+    if (sqrt(fabs(di)) < ks->conv) ks->conv_flag = 1;
+    else if (!isfinite(di)) ks->conv_flag = 3;
+    else if (ks->iter >= ks->maxit) ks->conv_flag = 2;
+    else ks->conv_flag = 0;
+  }
+}
+
 // The FP64 outer residual of the refinement: r = b - q (q = A x by the FP64
 // operator) and out = (r, m r), with |m| when absval.
 __global__ void __launch_bounds__(256)
@@ -1833,6 +1867,13 @@ cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const doubl
                                                 counter, V32.c);
   k_minres_update<<<vec_grid(n), 256, 0, s>>>(n, V.x, V.z0, V.w0, V.w00, V.v0, V.v, V.p,
                                                V.z, ks);
+  return cudaGetLastError();
+}
+
+cudaError_t pcgc_replace(int n, const double* b, const double* q, const double* m,
+                         KrylovVecs& V, KrylovScalars* ks, double* partial, unsigned* counter,
+                         cudaStream_t s) {
+  k_pcgc_replace<<<vec_grid(n), 256, 0, s>>>(n, b, q, m, V.r, V.z, ks, partial, counter);
   return cudaGetLastError();
 }
 

@@ -41,9 +41,12 @@ from poromec_gb300 import meshgen  # noqa: E402
 BENCH = dict(maxnlit=500, tol=1e-4, stop_crit=1, precond=2, solvtol=1e-10, maxit=200000)
 TIGHT = dict(BENCH, solvtol=1e-13)
 THREADS = os.cpu_count()
-# mean PCG iterations per step against the oracle's: within 3 % in FP64; the
-# compensated operator's refinement may add a correction sweep
-ITS_BAR = {pg.capi.PM_FP64: 0.03, pg.capi.PM_FP32C_REFINE: 0.5}
+# mean Krylov iterations per step against the oracle's: within 3 % in FP64.
+# PCG on the compensated operator replaces its residual by the FP64 one and
+# goes on (a few per cent more); rpsqmr on it restarts for each correction
+# sweep, which costs up to 65 % more iterations on the tetra box at 1e-10
+ITS_BAR = {(1, pg.capi.PM_FP64): 0.03, (1, pg.capi.PM_FP32C_REFINE): 0.1,
+           (11, pg.capi.PM_FP64): 0.03, (11, pg.capi.PM_FP32C_REFINE): 1.0}
 
 
 def _oracle(pb):
@@ -108,7 +111,7 @@ def test_cube_history_bench_settings(cube16, mode):
     """The 16^3 cube, 50 steps with the bench's settings (PCG 1e-10)."""
     pb, ref = cube16
     gpu = _gpu_history(pb, 50, 1, BENCH, mode)
-    worst = _compare(gpu, ref, 500 * BENCH["solvtol"], ITS_BAR[mode])
+    worst = _compare(gpu, ref, 500 * BENCH["solvtol"], ITS_BAR[1, mode])
     print("cube 16^3, 50 steps, mode %d: max rel. difference u %.2e p %.2e" % (mode, *worst))
 
 
@@ -135,7 +138,7 @@ def test_tetra_history_bench_settings(tetra8, mode):
     30 steps of rpsqmr with the bench's settings."""
     pb, ref = tetra8
     gpu = _gpu_history(pb, 30, 11, BENCH, mode)
-    worst = _compare(gpu, ref, 500 * BENCH["solvtol"], ITS_BAR[mode])
+    worst = _compare(gpu, ref, 500 * BENCH["solvtol"], ITS_BAR[11, mode])
     print("tetra 8^3, 30 steps, mode %d: u %.2e p %.2e" % (mode, *worst))
 
 
