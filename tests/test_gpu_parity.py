@@ -291,6 +291,7 @@ def test_rcm_numbering_pattern_and_values_match_oracle(problems):
         o = oracle.Oracle(int(pb["nnode"]), int(pb["nnodev"]), int(pb["numel"]),
                           int(pb["nen"]), int(pb["nenv"]), pb["ix"], pb["id"], pb["fnno"],
                           pb["x"], pb["ie"], pb["e"], num=num_o)
+        o.set_env(pb["gravity"], float(pb["dt"]))  # dt enters the pressure block
         assert m.neq == o.neq and m.nad == o.nad
         assert np.array_equal(m.get_id(), o.get_id())
         du = rng.standard_normal((m.nnode, 4)) * 1e-3
