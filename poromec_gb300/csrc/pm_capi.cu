@@ -484,23 +484,26 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       // pcg's test, it is replaced by the FP64 residual of the current x;
       // the iteration then goes on with the same search direction until the
       // replaced residual itself meets the test (the refinement of the FP64
-      // solve, without restarting the Krylov space).  Near the FP64
-      // operator's attainable accuracy (tolerances of 1e-13) the continued
-      // iteration stops gaining: after the recursive test has been met twice
-      // without the FP64 residual meeting it, the remaining correction is
-      // solved by restarted sweeps, A dx = b - A x to the same absolute
-      // target, x += dx.
+      // solve, without restarting the Krylov space).  Once the recursive
+      // test is met, the search direction has done its work: if the FP64
+      // residual misses the test there (or the recurrence breaks down, as it
+      // can on small systems whose Krylov space is exhausted), the remaining
+      // correction is solved by restarted sweeps, A dx = b - A x to the same
+      // absolute target, x += dx.
       constexpr double kDrop = 1e-4;
       constexpr int kMaxReplace = 256, kMaxSweeps = 8;
       double d_ref = -1.0;
-      int misses = 0;
       bool restart = false;
       for (;;) {
         PM_CUDA(cudaGraphLaunch(*g, h->stream));
         h->launches += 3 * kGraphIters;
         PM_TRY(read_scalars(h, &ks));
         if (d_ref < 0.0) d_ref = std::fabs(ks.bmb);
-        if (ks.conv_flag == 2 || ks.conv_flag == 3) break;
+        if (ks.conv_flag == 2) break;
+        if (ks.conv_flag == 3) {  // x holds the last finite iterate
+          restart = d_x != V.x;
+          break;
+        }
         const bool met = ks.conv_flag == 1;
         if (!met && std::fabs(ks.d) > kDrop * d_ref) continue;
         h->launches += 2;
@@ -514,7 +517,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
                   sweeps, ks.iter, std::sqrt(std::fabs(ks.d)), ks.conv);
         d_ref = std::fabs(ks.d);
         if (ks.conv_flag != 0) break;
-        if ((met && ++misses >= 2) || sweeps >= kMaxReplace) {
+        if (met || sweeps >= kMaxReplace) {
           restart = d_x != V.x;
           if (!restart) ks.conv_flag = 2;
           break;

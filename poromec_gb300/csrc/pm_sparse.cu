@@ -182,6 +182,11 @@ __global__ void __launch_bounds__(256)
                  KrylovScalars* ks, double* partial, unsigned* counter) {
   if (krylov_skip(ks, false)) return;
   const double alpha = ks->alpha;
+  if (!isfinite(alpha)) {
+    // breakdown ((p, A p) = 0): stop with x at the last finite iterate
+    if (blockIdx.x == 0 && threadIdx.x == 0) ks->conv_flag = 3;
+    return;
+  }
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] = x[i] + alpha * p[i];
