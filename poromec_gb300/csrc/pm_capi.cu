@@ -488,8 +488,8 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       // test is met, the search direction has done its work: if the FP64
       // residual misses the test there (or the recurrence breaks down, as it
       // can on small systems whose Krylov space is exhausted), the remaining
-      // correction is solved by restarted sweeps, A dx = b - A x to the same
-      // absolute target, x += dx.
+      // correction is solved by restarted sweeps with the FP64 operator,
+      // A dx = b - A x to the same absolute target, x += dx.
       constexpr double kDrop = 1e-4;
       constexpr int kMaxReplace = 256, kMaxSweeps = 8;
       double d_ref = -1.0;
@@ -548,10 +548,19 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
           ks.conv_flag = 2;
           break;
         }
+        // the correction sits at the compensated operator's noise level:
+        // it is solved with the FP64 operator (pcg to the same absolute
+        // target, the tolerance rescaled to this right-hand side)
+        if (!h->pcg_graph) {
+          PM_TRY(capture(h, &h->pcg_graph, [&]() {
+            return pm::pcg_iteration(P, val64, n, h->D.m, V, h->D.ks, h->D.partial,
+                                     h->D.counter, h->stream);
+          }));
+        }
         h->launches += 1;
-        PM_CUDA(pm::pcgc_init(n, h->D.rr, h->D.m, V, V32, h->D.ks, tol, conv, maxit - total,
-                              h->D.partial, h->D.counter, h->stream));
-        PM_TRY(run_graph(h, *g, &ks));
+        PM_CUDA(pm::pcg_init(n, h->D.rr, h->D.m, V, h->D.ks, conv / std::sqrt(std::fabs(rn2)),
+                             maxit - total, h->D.partial, h->D.counter, h->stream));
+        PM_TRY(run_graph(h, h->pcg_graph, &ks));
         total += ks.iter;
         ++sweeps;
         if (ks.conv_flag != 1) break;
