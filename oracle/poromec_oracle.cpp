@@ -1208,10 +1208,16 @@ int pform(or_handle_s* h, int isw, bool lhs, bool rhs, const double* u,
     {
       std::vector<double> s((size_t)nst * nst), p(nst);
       for (int c = 0; c < h->numcolors; ++c) {
+        // a colour lists its elements in increasing order: the elements of
+        // a timing sample [e_begin, e_end) are one contiguous part of it,
+        // shared among the threads like a whole colour
+        const int* first = h->color_elems.data() + h->color_ptr[c];
+        const int* last = h->color_elems.data() + h->color_ptr[c + 1];
+        const int j0 = h->color_ptr[c] + (int)(std::lower_bound(first, last, e_begin) - first);
+        const int j1 = h->color_ptr[c] + (int)(std::lower_bound(first, last, e_end) - first);
 #pragma omp for schedule(static)
-        for (int jc = h->color_ptr[c]; jc < h->color_ptr[c + 1]; ++jc) {
+        for (int jc = j0; jc < j1; ++jc) {
           const int nel = h->color_elems[jc];
-          if (nel < e_begin || nel >= e_end) continue;
           const int st = body(nel, s, p);
           if (st != OR_OK) {
 #pragma omp critical
