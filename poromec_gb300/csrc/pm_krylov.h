@@ -183,8 +183,8 @@ constexpr int kCaShape = 90, kCsShape = 91;
 constexpr int kCsWarps = 8;                // consumer warps of the streamed kernel
 constexpr int kCsNodes = 2 * kCsWarps;     // nodes per batch (one per half-warp)
 constexpr int kCsMaxStages = 4;
-constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,  104, 112, 114,
-                              124, 214, 312, 314, 502, 511, 512, 514, 522, kCaShape, kCsShape};
+constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,
+                              104, 112, 114, 124, 214, 312, 314, kCaShape, kCsShape};
 cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
 cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s);
 // Dynamic shared memory of the record kernel for a given record size and

@@ -622,104 +622,13 @@ __device__ __forceinline__ void cf_rows(const float* __restrict__ h,
   }
 }
 
-// The same rows with the loads software-pipelined: the loads of trip k + 1
-// (x pairs gathered at column indices read two trips ahead, values and
-// corrections) are issued before the arithmetic of trip k, so each lane
-// keeps a trip of loads in flight while it computes instead of alternating
-// between waiting and computing.  Twice the load registers of cf_rows.
-template <int D, int S, int U, bool PK>
-__device__ __forceinline__ void cf_rows_pipe(const float* __restrict__ h,
-                                             const int8_t* __restrict__ l,
-                                             const int32_t* __restrict__ cols,
-                                             const float2* __restrict__ xp, int W, int t,
-                                             F2 (&a)[4]) {
-  constexpr int T = U * S;  // columns of one trip of the sub-warp
-  P2 pa[2] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
-  float2 xv[U];
-  float hv[U][D];
-  int lv[U][D];
-  int cn[U];
-  {
-    int c0[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) c0[u] = (t + u * S < W) ? __ldcs(&cols[t + u * S]) : -1;
-#pragma unroll
-    for (int u = 0; u < U; ++u) xv[u] = c0[u] >= 0 ? xp[c0[u]] : make_float2(0.f, 0.f);
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        const bool ok = t + u * S < W;
-        hv[u][r] = ok ? __ldcs(&h[r * W + t + u * S]) : 0.f;
-        lv[u][r] = ok ? int(__ldcs(&l[r * W + t + u * S])) : 0;
-      }
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-      cn[u] = (t + T + u * S < W) ? __ldcs(&cols[t + T + u * S]) : -1;
-  }
-  for (int c = t; c < W; c += T) {
-    const int cq = c + T;
-    float2 xn[U];
-    float hn[U][D];
-    int ln[U][D];
-#pragma unroll
-    for (int u = 0; u < U; ++u) xn[u] = cn[u] >= 0 ? xp[cn[u]] : make_float2(0.f, 0.f);
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        const bool ok = cq + u * S < W;
-        hn[u][r] = ok ? __ldcs(&h[r * W + cq + u * S]) : 0.f;
-        ln[u][r] = ok ? int(__ldcs(&l[r * W + cq + u * S])) : 0;
-      }
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-      cn[u] = (cq + T + u * S < W) ? __ldcs(&cols[cq + T + u * S]) : -1;
-    if (PK) {
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const f2x xh = pk2(xv[u].x, xv[u].x), nxh = pk2(-xv[u].x, -xv[u].x);
-        const f2x xl = pk2(xv[u].y, xv[u].y);
-#pragma unroll
-        for (int k = 0; k < D / 2; ++k)
-          p2_fma(pa[k], pk2(hv[u][2 * k], hv[u][2 * k + 1]),
-                 p2_nqs(lv[u][2 * k], lv[u][2 * k + 1]), xh, nxh, xl);
-        if (D & 1) f2_fma(a[D - 1], hv[u][D - 1], lv[u][D - 1], xv[u].x, xv[u].y);
-      }
-    } else {
-#pragma unroll
-      for (int u = 0; u < U; ++u)
-#pragma unroll
-        for (int r = 0; r < D; ++r)
-          f2_fma(a[r], hv[u][r], lv[u][r], xv[u].x, xv[u].y);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      xv[u] = xn[u];
-#pragma unroll
-      for (int r = 0; r < D; ++r) {
-        hv[u][r] = hn[u][r];
-        lv[u][r] = ln[u][r];
-      }
-    }
-  }
-  if (PK) {
-#pragma unroll
-    for (int k = 0; k < D / 2; ++k) {
-      const float2 sn = up2(pa[k].sn), cn2 = up2(pa[k].cn), cp = up2(pa[k].cp);
-      a[2 * k] = F2{-sn.x, cp.x - cn2.x};
-      a[2 * k + 1] = F2{-sn.y, cp.y - cn2.y};
-    }
-  }
-}
-
 // MODE 0: y = A x.  MODE 1: PCG, alpha = d / (y . xd).  MODE 2: MINRES,
 // alpha = |xd . y| / beta^2.  xd is the FP64 operand whose pair is xp; y is
 // FP64.  S: lanes per node (8, 16 or 32), U: columns per lane and trip; both
 // chosen per matrix by the autotuner.  With S = 32 a warp reads each panel
 // row as full 128-byte lines; with S = 8 four nodes share a warp and each
 // load instruction touches four lines.
-template <int MODE, int S, int U, bool PK, int MINB, bool PIPE = false>
+template <int MODE, int S, int U, bool PK, int MINB>
 __global__ void __launch_bounds__(256, MINB)
     k_spmv_cf(PanelView P, const float* __restrict__ vh, const int8_t* __restrict__ vl,
               const float2* __restrict__ xp, double* __restrict__ y, const double* __restrict__ xd,
@@ -745,17 +654,10 @@ __global__ void __launch_bounds__(256, MINB)
       const float* h = vh + vo;
       const int8_t* l = vl + vo;
       const int32_t* cols = P.cols + P.col_off[node];
-      if (PIPE) {
-        if (d == 4) cf_rows_pipe<4, S, U, PK>(h, l, cols, xp, W, t, a);
-        else if (d == 3) cf_rows_pipe<3, S, U, PK>(h, l, cols, xp, W, t, a);
-        else if (d == 2) cf_rows_pipe<2, S, U, PK>(h, l, cols, xp, W, t, a);
-        else cf_rows_pipe<1, S, U, PK>(h, l, cols, xp, W, t, a);
-      } else {
-        if (d == 4) cf_rows<4, S, U, PK>(h, l, cols, xp, W, t, a);
-        else if (d == 3) cf_rows<3, S, U, PK>(h, l, cols, xp, W, t, a);
-        else if (d == 2) cf_rows<2, S, U, PK>(h, l, cols, xp, W, t, a);
-        else cf_rows<1, S, U, PK>(h, l, cols, xp, W, t, a);
-      }
+      if (d == 4) cf_rows<4, S, U, PK>(h, l, cols, xp, W, t, a);
+      else if (d == 3) cf_rows<3, S, U, PK>(h, l, cols, xp, W, t, a);
+      else if (d == 2) cf_rows<2, S, U, PK>(h, l, cols, xp, W, t, a);
+      else cf_rows<1, S, U, PK>(h, l, cols, xp, W, t, a);
     }
     // transposed butterfly on (sum, correction) pairs over the S lanes: the
     // first two levels halve the rows each lane carries, the rest add
@@ -1771,11 +1673,11 @@ int resident_grid(K kernel) {
   return g < kRedBlocks ? g : kRedBlocks;
 }
 
-template <int MODE, int S, int U, bool PK = false, int MINB = 1, bool PIPE = false>
+template <int MODE, int S, int U, bool PK = false, int MINB = 1>
 void launch_cf(const PanelView& P, CompVals C, const float2* xp, double* y, const double* xd,
                KrylovScalars* ks, double* partial, unsigned* counter, cudaStream_t s) {
-  static const int grid = resident_grid(k_spmv_cf<MODE, S, U, PK, MINB, PIPE>);
-  k_spmv_cf<MODE, S, U, PK, MINB, PIPE><<<grid, 256, 0, s>>>(
+  static const int grid = resident_grid(k_spmv_cf<MODE, S, U, PK, MINB>);
+  k_spmv_cf<MODE, S, U, PK, MINB><<<grid, 256, 0, s>>>(
       P, C.hi, C.lo, xp, y, xd, ks, partial, counter);
 }
 
@@ -1915,12 +1817,6 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
     case 214: launch_cf<MODE, 16, 4, false, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 314: launch_cf<MODE, 16, 4, true, 3>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 312: launch_cf<MODE, 16, 2, true, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
-    // software-pipelined loads (cf_rows_pipe)
-    case 502: launch_cf<MODE, 8, 2, true, 3, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
-    case 511: launch_cf<MODE, 16, 1, true, 4, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
-    case 512: launch_cf<MODE, 16, 2, true, 3, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
-    case 514: launch_cf<MODE, 16, 4, true, 2, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
-    case 522: launch_cf<MODE, 32, 2, true, 3, true>(P, C, xp, y, xd, ks, partial, counter, s); break;
     default: launch_cf<MODE, 8, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;
   }
 }
