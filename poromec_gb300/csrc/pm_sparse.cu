@@ -730,97 +730,67 @@ __device__ __forceinline__ float f4c(const float4& v, int c) {
   return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
 }
 
-// One node's rows on S lanes, in two passes over the lanes' steps.
-// Own blocks (rows = the node's dofs, columns = the neighbour's; contiguous
-// rows from row0, streamed and left in L2 for their second read): the rows
-// and the neighbour ref of step j + S are loaded before the arithmetic of
-// step j, whose x pairs wait for its ref only.  Lower neighbours' blocks,
-// read transposed (rows = the neighbour's dofs, columns = the node's own;
-// the block's last read): the ref of the next step is loaded ahead.
-// Blocks are rows of four (zero padding), the node's d <= 4 rows taken as
-// four; both passes accumulate into the node's rows, two rows per packed
-// f32x2 instruction.
-__device__ __forceinline__ void sb_own_step(P2 (&pa)[2], const float4 (&bo)[4],
-                                            const int (&wo)[4], const float2 (&xo)[4]) {
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const f2x xh = pk2(xo[c].x, xo[c].x), nxh = pk2(-xo[c].x, -xo[c].x);
-    const f2x xl = pk2(xo[c].y, xo[c].y);
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-      p2_fma(pa[k], pk2(f4c(bo[2 * k], c), f4c(bo[2 * k + 1], c)),
-             p2_nqs(sb_q(wo[2 * k], c), sb_q(wo[2 * k + 1], c)), xh, nxh, xl);
-  }
-}
-
+// One node's rows on S lanes.  Step j of a lane takes its node's j-th own
+// block (rows = the node's dofs, columns = the neighbour's; contiguous rows
+// from row0, streamed and left in L2 for the second read) and its j-th
+// lower neighbour's stored block read transposed (rows = the neighbour's
+// dofs, columns = the node's own; that read is the block's last), with the
+// loads of both issued before their arithmetic.  Blocks are rows of four
+// (zero padding), the node's d <= 4 rows taken as four; both kinds
+// accumulate into the node's rows, two rows per packed f32x2 instruction.
 template <int S>
 __device__ __forceinline__ void sb_rows(const CompVals& C, int d, int row0, int own0,
                                         int own1, int tr0, int tr1,
                                         const float2* __restrict__ xp, int t, F2 (&a)[4]) {
   P2 pa[2] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
   const int nown = own1 - own0, ntr = tr1 - tr0;
-  {
-    float4 bo[4];
-    int wo[4];
-    int no = 0;
-    if (t < nown) {
-      no = __ldcs(&C.sb_own[own0 + t]);
+  const int nmax = nown > ntr ? nown : ntr;
+  for (int j = t; j < nmax; j += S) {
+    const bool ho = j < nown, ht = j < ntr;
+    const int no = ho ? __ldcs(&C.sb_own[own0 + j]) : 0;
+    const int2 rt = ht ? __ldcs(&C.sb_tr[tr0 + j]) : make_int2(0, 0);
+    const int dl = ho ? d : 0;
+    const int rowo = row0 + j * d;
+    float4 bo[4], bt[4];
+    int wo[4], wt[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        bo[r] = r < d ? __ldcg(&C.sb_hi[row0 + t * d + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-        wo[r] = r < d ? __ldcg(&C.sb_lo[row0 + t * d + r]) : 0;
-      }
+    for (int r = 0; r < 4; ++r) {
+      bo[r] = r < dl ? __ldcg(&C.sb_hi[rowo + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      wo[r] = r < dl ? __ldcg(&C.sb_lo[rowo + r]) : 0;
     }
-    for (int j = t; j < nown; j += S) {
-      const int eqo = no & 0x7ffffff, dno = (no >> 27) & 7;
-      float2 xo[4];
+    const int eqo = no & 0x7ffffff, dno = ho ? (no >> 27) & 7 : 0;
+    const int eqt = rt.y & 0x7ffffff, dnt = ht ? (rt.y >> 27) & 7 : 0;
+    float2 xo[4], xt[4];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) xo[c] = c < dno ? xp[eqo + c] : make_float2(0.f, 0.f);
-      float4 bc[4];
-      int wc[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        bc[r] = bo[r];
-        wc[r] = wo[r];
-      }
-      const int jn = j + S;
-      if (jn < nown) {
-        no = __ldcs(&C.sb_own[own0 + jn]);
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          bo[r] = r < d ? __ldcg(&C.sb_hi[row0 + jn * d + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-          wo[r] = r < d ? __ldcg(&C.sb_lo[row0 + jn * d + r]) : 0;
-        }
-      }
-      sb_own_step(pa, bc, wc, xo);
+    for (int c = 0; c < 4; ++c) {
+      xo[c] = c < dno ? xp[eqo + c] : make_float2(0.f, 0.f);
+      xt[c] = c < dnt ? xp[eqt + c] : make_float2(0.f, 0.f);
     }
-  }
-  {
-    int2 rt = t < ntr ? __ldcs(&C.sb_tr[tr0 + t]) : make_int2(0, 0);
-    for (int j = t; j < ntr; j += S) {
-      const int eqt = rt.y & 0x7ffffff, dnt = (rt.y >> 27) & 7;
-      const int rowt = rt.x;
-      rt = j + S < ntr ? __ldcs(&C.sb_tr[tr0 + j + S]) : make_int2(0, 0);
-      float4 bt[4];
-      int wt[4];
-      float2 xt[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        bt[r] = r < dnt ? __ldcs(&C.sb_hi[rowt + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-        wt[r] = r < dnt ? __ldcs(&C.sb_lo[rowt + r]) : 0;
-        xt[r] = r < dnt ? xp[eqt + r] : make_float2(0.f, 0.f);
-      }
-      // the node's rows (2k, 2k+1) are columns of the neighbour's row r,
-      // times the neighbour's x[r]
+    for (int r = 0; r < 4; ++r) {
+      bt[r] = r < dnt ? __ldcs(&C.sb_hi[rt.x + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      wt[r] = r < dnt ? __ldcs(&C.sb_lo[rt.x + r]) : 0;
+    }
+    // own block: rows (2k, 2k+1) of the node times the neighbour's x[c]
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const f2x xh = pk2(xt[r].x, xt[r].x), nxh = pk2(-xt[r].x, -xt[r].x);
-        const f2x xl = pk2(xt[r].y, xt[r].y);
+    for (int c = 0; c < 4; ++c) {
+      const f2x xh = pk2(xo[c].x, xo[c].x), nxh = pk2(-xo[c].x, -xo[c].x);
+      const f2x xl = pk2(xo[c].y, xo[c].y);
 #pragma unroll
-        for (int k = 0; k < 2; ++k)
-          p2_fma(pa[k], pk2(f4c(bt[r], 2 * k), f4c(bt[r], 2 * k + 1)),
-                 p2_nqs(sb_q(wt[r], 2 * k), sb_q(wt[r], 2 * k + 1)), xh, nxh, xl);
-      }
+      for (int k = 0; k < 2; ++k)
+        p2_fma(pa[k], pk2(f4c(bo[2 * k], c), f4c(bo[2 * k + 1], c)),
+               p2_nqs(sb_q(wo[2 * k], c), sb_q(wo[2 * k + 1], c)), xh, nxh, xl);
+    }
+    // lower neighbour's block transposed: the node's rows (2k, 2k+1) are
+    // columns of the neighbour's row r, times the neighbour's x[r]
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const f2x xh = pk2(xt[r].x, xt[r].x), nxh = pk2(-xt[r].x, -xt[r].x);
+      const f2x xl = pk2(xt[r].y, xt[r].y);
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+        p2_fma(pa[k], pk2(f4c(bt[r], 2 * k), f4c(bt[r], 2 * k + 1)),
+               p2_nqs(sb_q(wt[r], 2 * k), sb_q(wt[r], 2 * k + 1)), xh, nxh, xl);
     }
   }
 #pragma unroll
