@@ -1273,8 +1273,7 @@ void free_all(Handle* h) {
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
                   P.val32, P.valh, P.vall, P.rec, P.rec_off, P.node_val_off, P.node_W,
                   P.order, P.cs_desc, P.cs_batch_slot, P.cs_batch_off, P.cs_batch_bytes,
-                  P.cs_cta_batch, P.fault, P.sb_hi, P.sb_lo, P.sb_own, P.sb_tr, P.sb_node,
-                  P.sb_build};
+                  P.cs_cta_batch, P.fault, P.sb_hi, P.sb_lo, P.sb_ref, P.sb_node, P.sb_build};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})

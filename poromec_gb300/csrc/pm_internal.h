@@ -60,8 +60,7 @@ struct Panels {
   // symmetric block layout (CompVals, shape kSbShape) and its build list
   float4* sb_hi = nullptr;
   int* sb_lo = nullptr;
-  int* sb_own = nullptr;
-  int2* sb_tr = nullptr;
+  int2* sb_ref = nullptr;
   int4* sb_node = nullptr;
   int4* sb_build = nullptr;
   int64_t sb_nblocks = 0;
@@ -83,8 +82,8 @@ struct Panels {
     return CompVals{valh,          vall,          rec,          rec_off,        rec_max,
                     ca_warps,      ca_grid,       cs_desc,      cs_batch_slot,  cs_batch_off,
                     cs_batch_bytes, cs_cta_batch, cs_grid,      cs_nstage,      cs_stage_bytes,
-                    fault,         shape,         sb_hi,        sb_lo,          sb_own,
-                    sb_tr,         sb_node,       sb_nslots};
+                    fault,         shape,         sb_hi,        sb_lo,          sb_ref,
+                    sb_node,       sb_nslots};
   }
 };
 

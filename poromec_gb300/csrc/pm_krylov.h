@@ -180,24 +180,22 @@ struct CompVals {
               // kernel; kSbShape, + 1, + 2: the symmetric block kernel with
               // 8, 16, 32 lanes per node; + 3, + 4: 16 and 8 lanes held to 3
               // CTAs per SM
-  // Symmetric block layout (shape kSbShape): each off-diagonal node block
-  // stored once, under the node with the lower equations, with the diagonal
-  // blocks.  The block of row node a and column node b (eq0_b >= eq0_a) is
-  // d_a rows of four FP32 hi values (b's d_b columns, zero-padded) in sb_hi
-  // and four int8 corrections per row packed in one int in sb_lo.  Nodes are
-  // visited in equation order (sorted by dofs within runs of 1024), a few
-  // lanes each; slot s has sb_node[s] = {eq0 | d << 27, first own block row,
-  // first own ref, first transposed ref} (sb_node[nslots] ends the lists).
-  // A node's own blocks are contiguous rows, each with a ref in sb_own (the
-  // neighbour's eq0 | d << 27, for its x); sb_tr lists the blocks of its lower
-  // neighbours, {first block row, the neighbour's eq0 | d << 27}, read
-  // transposed.  A block is streamed by its lower node and read again by the
-  // upper one shortly after, mostly from L2; rows are summed by one node's
-  // lanes in a fixed order, so the product is deterministic without atomics.
+  // Symmetric block layout (shape kSbShape): the lower triangle and the
+  // diagonal stored once, as node blocks.  The block of row node a and
+  // column node b (eq0_b <= eq0_a) is d_a rows of four FP32 hi values
+  // (b's d_b columns, zero-padded) in sb_hi and four int8 corrections per
+  // row packed in one int in sb_lo.  Nodes are visited in equation order,
+  // one warp each; slot s has sb_node[s] = {eq0, d, first ref, first upper
+  // ref} (sb_node[nslots].z = end of its refs), and each ref is
+  // {first block row, eq0_nb | d_nb << 27 | transposed << 30}: a lower or
+  // diagonal block of the node itself (rows = the node's dofs) or an upper
+  // one, the stored block of the neighbour read transposed.  Every block is
+  // read by its two nodes, the second read mostly from L2 (equation order
+  // keeps neighbours close in time); rows are summed by one warp in a fixed
+  // order, so the product is deterministic without atomics.
   const float4* sb_hi;
   const int* sb_lo;
-  const int* sb_own;
-  const int2* sb_tr;
+  const int2* sb_ref;
   const int4* sb_node;
   int sb_nslots;
 };

@@ -388,133 +388,141 @@ int build_rec_layout(Handle* h) {
 
 // Symmetric block layout of the compensated operator (CompVals, shape
 // kSbShape).  From the panels: each panel's columns are runs of its
-// neighbours' consecutive equations.  A node's own blocks are the runs from
-// its own equations on (the diagonal block and the blocks of its upper
-// neighbours), stored once under it, contiguous in the visiting order; a
-// node reads the blocks of its lower neighbours transposed, where those
-// stored them.  Visiting in equation order, a block is first streamed by the
-// lower node and read again by the upper one shortly after, mostly from L2.
+// neighbours' consecutive equations; the runs of equations up to the node's
+// own are its lower and diagonal blocks, stored once under the node (rows
+// assigned in equation order); every node refers to its own lower blocks
+// and, transposed, to the lower blocks of its upper neighbours.
 int build_sb_layout(Handle* h) {
   Panels& P = h->P;
   const int nact = P.nact;
-  if (nact == 0 || h->neq >= (1 << 27)) return PM_OK;  // refs encode eq0 < 2^27
+  if (nact == 0 || h->neq >= (1 << 27)) return PM_OK;  // the ref encoding needs eq0 < 2^27
   std::vector<int32_t> eqnode(h->neq, -1);
   for (int k = 0; k < nact; ++k)
     for (int q = 0; q < h->h_d[k]; ++q) eqnode[h->h_eq0[k] + q] = k;
-  auto runs_of = [&](int k, int j0, int j1, auto&& fn) {
-    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
-    for (int j = j0; j < j1; ++j)
-      if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) fn(eqnode[c[j]], j);
-  };
-  // own runs of every node: (neighbour, first panel column)
-  std::vector<int64_t> own_ptr(nact + 1, 0);
-  std::vector<int32_t> ntr(nact, 0);
-  for (int k = 0; k < nact; ++k) {
-    int n = 0;
-    runs_of(k, h->h_low[k], h->h_W[k], [&](int, int) { ++n; });
-    own_ptr[k + 1] = n;
-    int m = 0;
-    runs_of(k, 0, h->h_low[k], [&](int, int) { ++m; });
-    ntr[k] = m;
-  }
-  for (int k = 0; k < nact; ++k) own_ptr[k + 1] += own_ptr[k];
-  const int64_t nblocks = own_ptr[nact];
-  std::vector<int32_t> own_nb(nblocks), own_col(nblocks), own_row(nblocks);
-  for (int k = 0; k < nact; ++k) {
-    int64_t r = own_ptr[k];
-    runs_of(k, h->h_low[k], h->h_W[k], [&](int m, int j) {
-      own_nb[r] = m;
-      own_col[r] = j;
-      ++r;
-    });
-  }
-  // visiting slots: equation order, and within runs of 1024 slots by free
-  // dofs and block count, so that the nodes sharing a warp run alike
   std::vector<int32_t> slot_node(nact);
   std::iota(slot_node.begin(), slot_node.end(), 0);
   std::sort(slot_node.begin(), slot_node.end(),
             [&](int a, int b) { return h->h_eq0[a] < h->h_eq0[b]; });
-  constexpr int kRun = 1024;
-  for (int i0 = 0; i0 < nact; i0 += kRun) {
-    const int i1 = std::min(nact, i0 + kRun);
-    std::stable_sort(slot_node.begin() + i0, slot_node.begin() + i1, [&](int a, int b) {
-      if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
-      const int64_t na = own_ptr[a + 1] - own_ptr[a] + ntr[a];
-      const int64_t nb = own_ptr[b + 1] - own_ptr[b] + ntr[b];
-      return na > nb;
-    });
+  // lower runs of every node: (neighbour, first panel column), stored rows
+  std::vector<int64_t> low_ptr(nact + 1, 0);
+  for (int k = 0; k < nact; ++k) {
+    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
+    const int n = h->h_low[k] + h->h_d[k];
+    int runs = 0;
+    for (int j = 0; j < n; ++j)
+      if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) ++runs;
+    low_ptr[k + 1] = runs;
   }
-  // block rows in the visiting order: a node's own blocks are contiguous
+  for (int k = 0; k < nact; ++k) low_ptr[k + 1] += low_ptr[k];
+  const int64_t nblocks = low_ptr[nact];
+  std::vector<int32_t> low_nb(nblocks), low_col(nblocks), low_row(nblocks);
+  for (int k = 0; k < nact; ++k) {
+    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
+    const int n = h->h_low[k] + h->h_d[k];
+    int64_t r = low_ptr[k];
+    for (int j = 0; j < n; ++j)
+      if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) {
+        low_nb[r] = eqnode[c[j]];
+        low_col[r] = j;
+        ++r;
+      }
+  }
+  // visiting slots: equation order (which keeps the two reads of a block
+  // close in time, for L2), and within runs of 1024 slots by free dofs and
+  // block count, so that the nodes sharing a warp run alike
+  {
+    std::vector<int32_t> nblk(nact, 0);
+    for (int k = 0; k < nact; ++k) {
+      const int32_t* c = h->h_cols.data() + h->h_col_off[k];
+      int runs = 0;
+      for (int j = 0; j < h->h_W[k]; ++j)
+        if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) ++runs;
+      nblk[k] = runs;
+    }
+    constexpr int kRun = 1024;
+    for (int i0 = 0; i0 < nact; i0 += kRun) {
+      const int i1 = std::min(nact, i0 + kRun);
+      std::stable_sort(slot_node.begin() + i0, slot_node.begin() + i1, [&](int a, int b) {
+        if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
+        return nblk[a] > nblk[b];
+      });
+    }
+  }
+  // block rows in the visiting order, so that a node's own blocks are
+  // contiguous and the stream of them follows the visit
   int64_t rows = 0;
-  std::vector<int32_t> row0(nact);
   for (int i = 0; i < nact; ++i) {
     const int k = slot_node[i];
-    row0[k] = (int32_t)rows;
-    for (int64_t r = own_ptr[k]; r < own_ptr[k + 1]; ++r) {
-      own_row[r] = (int32_t)rows;
+    for (int64_t r = low_ptr[k]; r < low_ptr[k + 1]; ++r) {
+      low_row[r] = (int32_t)rows;
       rows += h->h_d[k];
+      if (rows >= (int64_t)1 << 31) return PM_OK;  // row indices are int32
     }
-    if (rows >= (int64_t)1 << 31) return PM_OK;  // block rows are int32
   }
   std::vector<int4> build(nblocks);
   for (int k = 0; k < nact; ++k)
-    for (int64_t r = own_ptr[k]; r < own_ptr[k + 1]; ++r)
-      build[r] = make_int4(k, own_col[r], own_row[r], h->h_d[own_nb[r]]);
-  auto enc = [&](int m) {
-    return (int)((unsigned)h->h_eq0[m] | ((unsigned)h->h_d[m] << 27));
-  };
-  // per slot: the neighbours of its own blocks (x gathers), and the
-  // transposed reads of its lower neighbours' blocks
-  std::vector<int64_t> own_ref(nact + 1, 0), tr_ref(nact + 1, 0);
+    for (int64_t r = low_ptr[k]; r < low_ptr[k + 1]; ++r)
+      build[r] = make_int4(k, low_col[r], low_row[r], h->h_d[low_nb[r]]);
+  // refs per slot: own lower blocks, then the upper neighbours' blocks
+  std::vector<int4> node(nact + 1);
+  std::vector<int64_t> ref_ptr(nact + 1, 0);
   for (int i = 0; i < nact; ++i) {
     const int k = slot_node[i];
-    own_ref[i + 1] = own_ref[i] + (own_ptr[k + 1] - own_ptr[k]);
-    tr_ref[i + 1] = tr_ref[i] + ntr[k];
+    int upper = 0;
+    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
+    for (int j = h->h_low[k] + h->h_d[k]; j < h->h_W[k]; ++j)
+      if (eqnode[c[j]] != eqnode[c[j - 1]]) ++upper;
+    ref_ptr[i + 1] = ref_ptr[i] + (low_ptr[k + 1] - low_ptr[k]) + upper;
   }
-  if (tr_ref[nact] >= (int64_t)1 << 31 || own_ref[nact] >= (int64_t)1 << 31) return PM_OK;
-  std::vector<int32_t> own(own_ref[nact]);
-  std::vector<int2> tr(tr_ref[nact]);
-  std::vector<int4> node(nact + 1);
+  if (ref_ptr[nact] >= (int64_t)1 << 31) return PM_OK;
+  std::vector<int2> ref(ref_ptr[nact]);
+  auto enc = [&](int m, int transposed) {
+    return (int)((unsigned)h->h_eq0[m] | ((unsigned)h->h_d[m] << 27) |
+                 ((unsigned)transposed << 30));
+  };
   int bad = 0;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : bad)
   for (int i = 0; i < nact; ++i) {
     const int k = slot_node[i];
-    int64_t o = own_ref[i];
-    for (int64_t r = own_ptr[k]; r < own_ptr[k + 1]; ++r) own[o++] = enc(own_nb[r]);
-    int64_t t = tr_ref[i];
-    runs_of(k, 0, h->h_low[k], [&](int m, int) {
-      // k's block among m's own runs (sorted by equation)
-      int64_t lo = own_ptr[m], hi = own_ptr[m + 1];
+    int64_t o = ref_ptr[i];
+    for (int64_t r = low_ptr[k]; r < low_ptr[k + 1]; ++r)
+      ref[o++] = make_int2(low_row[r], enc(low_nb[r], 0));
+    const int64_t up = o;
+    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
+    for (int j = h->h_low[k] + h->h_d[k]; j < h->h_W[k]; ++j) {
+      if (eqnode[c[j]] == eqnode[c[j - 1]]) continue;
+      const int m = eqnode[c[j]];
+      // k's block in m's lower runs (sorted by equation)
+      int64_t lo = low_ptr[m], hi = low_ptr[m + 1];
       while (lo < hi) {
         const int64_t mid = (lo + hi) / 2;
-        if (h->h_eq0[own_nb[mid]] < h->h_eq0[k]) lo = mid + 1;
+        if (h->h_eq0[low_nb[mid]] < h->h_eq0[k]) lo = mid + 1;
         else hi = mid;
       }
-      if (lo >= own_ptr[m + 1] || own_nb[lo] != k) {
+      if (lo >= low_ptr[m + 1] || low_nb[lo] != k) {
         ++bad;
-        return;
+        continue;
       }
-      tr[t++] = make_int2(own_row[lo], enc(m));
-    });
-    node[i] = make_int4(enc(k), row0[k], (int)own_ref[i], (int)tr_ref[i]);
+      ref[o++] = make_int2(low_row[lo], enc(m, 1));
+    }
+    node[i] = make_int4(h->h_eq0[k], h->h_d[k], (int)ref_ptr[i], (int)up);
   }
   if (bad) {  // an unsymmetric pattern: leave the layout out
     if (getenv("PM_DEBUG")) fprintf(stderr, "symmetric block layout: %d unmatched blocks\n", bad);
     return PM_OK;
   }
-  node[nact] = make_int4(0, (int)rows, (int)own_ref[nact], (int)tr_ref[nact]);
+  node[nact] = make_int4(0, 0, (int)ref_ptr[nact], (int)ref_ptr[nact]);
   int st;
   if ((st = upload<float4>(h, &P.sb_hi, nullptr, (size_t)rows))) return st;
   if ((st = upload<int>(h, &P.sb_lo, nullptr, (size_t)rows))) return st;
-  if ((st = upload(h, &P.sb_own, own.data(), own.size()))) return st;
-  if ((st = upload(h, &P.sb_tr, tr.data(), tr.size()))) return st;
+  if ((st = upload(h, &P.sb_ref, ref.data(), ref.size()))) return st;
   if ((st = upload(h, &P.sb_node, node.data(), node.size()))) return st;
   if ((st = upload(h, &P.sb_build, build.data(), build.size()))) return st;
   P.sb_nblocks = nblocks;
   P.sb_nslots = nact;
   if (getenv("PM_DEBUG"))
-    fprintf(stderr, "symmetric block layout: %lld blocks, %lld rows, %lld transposed reads\n",
-            (long long)nblocks, (long long)rows, (long long)tr_ref[nact]);
+    fprintf(stderr, "symmetric block layout: %lld blocks, %lld rows, %lld refs\n",
+            (long long)nblocks, (long long)rows, (long long)ref_ptr[nact]);
   return PM_OK;
 }
 

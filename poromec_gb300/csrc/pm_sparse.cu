@@ -731,66 +731,67 @@ __device__ __forceinline__ float f4c(const float4& v, int c) {
 }
 
 // One node's rows on S lanes.  Step j of a lane takes its node's j-th own
-// block (rows = the node's dofs, columns = the neighbour's; contiguous rows
-// from row0, streamed and left in L2 for the second read) and its j-th
-// lower neighbour's stored block read transposed (rows = the neighbour's
-// dofs, columns = the node's own; that read is the block's last), with the
-// loads of both issued before their arithmetic.  Blocks are rows of four
-// (zero padding), the node's d <= 4 rows taken as four; both kinds
-// accumulate into the node's rows, two rows per packed f32x2 instruction.
+// lower or diagonal block (rows = the node's dofs, columns = the
+// neighbour's) and its j-th upper neighbour's stored block read transposed
+// (rows = the neighbour's dofs, columns = the node's own), with the loads of
+// both issued before their arithmetic.  Blocks are rows of four (zero
+// padding), the node's d <= 4 rows taken as four; both kinds accumulate into
+// the node's rows, two rows per packed f32x2 instruction.  Blocks are loaded
+// through L2 only (each is read by its two nodes); refs stream.
 template <int S>
-__device__ __forceinline__ void sb_rows(const CompVals& C, int d, int row0, int own0,
-                                        int own1, int tr0, int tr1,
-                                        const float2* __restrict__ xp, int t, F2 (&a)[4]) {
+__device__ __forceinline__ void sb_rows(const CompVals& C, int d, int ref0, int refup,
+                                        int ref1, const float2* __restrict__ xp, int t,
+                                        F2 (&a)[4]) {
   P2 pa[2] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
-  const int nown = own1 - own0, ntr = tr1 - tr0;
-  const int nmax = nown > ntr ? nown : ntr;
+  const int nlow = refup - ref0, nup = ref1 - refup;
+  const int nmax = nlow > nup ? nlow : nup;
+  // the refs of a lane's next step are loaded one step ahead, so that a
+  // step waits for one round trip (blocks and x) instead of two
+  int2 rln = t < nlow ? __ldcs(&C.sb_ref[ref0 + t]) : make_int2(0, 0);
+  int2 run = t < nup ? __ldcs(&C.sb_ref[refup + t]) : make_int2(0, 0);
   for (int j = t; j < nmax; j += S) {
-    const bool ho = j < nown, ht = j < ntr;
-    const int no = ho ? __ldcs(&C.sb_own[own0 + j]) : 0;
-    const int2 rt = ht ? __ldcs(&C.sb_tr[tr0 + j]) : make_int2(0, 0);
-    const int dl = ho ? d : 0;
-    const int rowo = row0 + j * d;
-    float4 bo[4], bt[4];
-    int wo[4], wt[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      bo[r] = r < dl ? __ldcg(&C.sb_hi[rowo + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      wo[r] = r < dl ? __ldcg(&C.sb_lo[rowo + r]) : 0;
-    }
-    const int eqo = no & 0x7ffffff, dno = ho ? (no >> 27) & 7 : 0;
-    const int eqt = rt.y & 0x7ffffff, dnt = ht ? (rt.y >> 27) & 7 : 0;
-    float2 xo[4], xt[4];
+    const bool hl = j < nlow, hu = j < nup;
+    const int2 rl = rln, ru = run;
+    rln = j + S < nlow ? __ldcs(&C.sb_ref[ref0 + j + S]) : make_int2(0, 0);
+    run = j + S < nup ? __ldcs(&C.sb_ref[refup + j + S]) : make_int2(0, 0);
+    const int eql = rl.y & 0x7ffffff, dnl = hl ? (rl.y >> 27) & 7 : 0;
+    const int equ = ru.y & 0x7ffffff, dnu = hu ? (ru.y >> 27) & 7 : 0;
+    const int dl = hl ? d : 0;
+    float2 xl[4], xu[4];
+    float4 bl[4], bu[4];
+    int wl[4], wu[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      xo[c] = c < dno ? xp[eqo + c] : make_float2(0.f, 0.f);
-      xt[c] = c < dnt ? xp[eqt + c] : make_float2(0.f, 0.f);
+      xl[c] = c < dnl ? xp[eql + c] : make_float2(0.f, 0.f);
+      xu[c] = c < dnu ? xp[equ + c] : make_float2(0.f, 0.f);
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      bt[r] = r < dnt ? __ldcs(&C.sb_hi[rt.x + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      wt[r] = r < dnt ? __ldcs(&C.sb_lo[rt.x + r]) : 0;
+      bl[r] = r < dl ? __ldcg(&C.sb_hi[rl.x + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      wl[r] = r < dl ? __ldcg(&C.sb_lo[rl.x + r]) : 0;
+      bu[r] = r < dnu ? __ldcg(&C.sb_hi[ru.x + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      wu[r] = r < dnu ? __ldcg(&C.sb_lo[ru.x + r]) : 0;
     }
     // own block: rows (2k, 2k+1) of the node times the neighbour's x[c]
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const f2x xh = pk2(xo[c].x, xo[c].x), nxh = pk2(-xo[c].x, -xo[c].x);
-      const f2x xl = pk2(xo[c].y, xo[c].y);
+      const f2x xh = pk2(xl[c].x, xl[c].x), nxh = pk2(-xl[c].x, -xl[c].x);
+      const f2x xo = pk2(xl[c].y, xl[c].y);
 #pragma unroll
       for (int k = 0; k < 2; ++k)
-        p2_fma(pa[k], pk2(f4c(bo[2 * k], c), f4c(bo[2 * k + 1], c)),
-               p2_nqs(sb_q(wo[2 * k], c), sb_q(wo[2 * k + 1], c)), xh, nxh, xl);
+        p2_fma(pa[k], pk2(f4c(bl[2 * k], c), f4c(bl[2 * k + 1], c)),
+               p2_nqs(sb_q(wl[2 * k], c), sb_q(wl[2 * k + 1], c)), xh, nxh, xo);
     }
-    // lower neighbour's block transposed: the node's rows (2k, 2k+1) are
-    // columns of the neighbour's row r, times the neighbour's x[r]
+    // upper block transposed: the node's rows (2k, 2k+1) are columns of
+    // the neighbour's row r, times the neighbour's x[r]
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const f2x xh = pk2(xt[r].x, xt[r].x), nxh = pk2(-xt[r].x, -xt[r].x);
-      const f2x xl = pk2(xt[r].y, xt[r].y);
+      const f2x xh = pk2(xu[r].x, xu[r].x), nxh = pk2(-xu[r].x, -xu[r].x);
+      const f2x xo = pk2(xu[r].y, xu[r].y);
 #pragma unroll
       for (int k = 0; k < 2; ++k)
-        p2_fma(pa[k], pk2(f4c(bt[r], 2 * k), f4c(bt[r], 2 * k + 1)),
-               p2_nqs(sb_q(wt[r], 2 * k), sb_q(wt[r], 2 * k + 1)), xh, nxh, xl);
+        p2_fma(pa[k], pk2(f4c(bu[r], 2 * k), f4c(bu[r], 2 * k + 1)),
+               p2_nqs(sb_q(wu[r], 2 * k), sb_q(wu[r], 2 * k + 1)), xh, nxh, xo);
     }
   }
 #pragma unroll
@@ -820,16 +821,14 @@ __global__ void __launch_bounds__(256, MINB)
   double dsum = 0.0;
   for (int base = warp * kNodesPerWarp; base < C.sb_nslots; base += nwarp * kNodesPerWarp) {
     const int sl = base + lane / S;
-    int4 nd = make_int4(0, 0, 0, 0), nx = make_int4(0, 0, 0, 0);
+    int4 nd = make_int4(0, 0, 0, 0);
+    int ref1 = 0;
     if (sl < C.sb_nslots) {
       nd = C.sb_node[sl];
-      nx = C.sb_node[sl + 1];
+      ref1 = C.sb_node[sl + 1].z;
     }
-    const int d = sl < C.sb_nslots ? (nd.x >> 27) & 7 : 0;
-    const int eq0 = nd.x & 0x7ffffff;
     F2 a[4];
-    sb_rows<S>(C, d, nd.y, nd.z, sl < C.sb_nslots ? nx.z : nd.z, nd.w,
-               sl < C.sb_nslots ? nx.w : nd.w, xp, t, a);
+    sb_rows<S>(C, nd.y, nd.z, nd.w, sl < C.sb_nslots ? ref1 : nd.w, xp, t, a);
     constexpr int o1 = S / 2, o2 = S / 4;
     const bool h1 = (t & o1) != 0, h2 = (t & o2) != 0;
     F2 k0 = h1 ? a[2] : a[0], k1 = h1 ? a[3] : a[1];
@@ -840,10 +839,10 @@ __global__ void __launch_bounds__(256, MINB)
 #pragma unroll
     for (int o = S / 8; o > 0; o >>= 1) k = f2_add(k, f2_shfl(k, o));
     const int r = (h1 ? 2 : 0) + (h2 ? 1 : 0);
-    if ((t & (o2 - 1)) == 0 && r < d) {
+    if ((t & (o2 - 1)) == 0 && r < nd.y) {
       const double v = double(k.s) + double(k.c);
-      y[eq0 + r] = v;
-      if (MODE != 0) dsum += v * xd[eq0 + r];
+      y[nd.x + r] = v;
+      if (MODE != 0) dsum += v * xd[nd.x + r];
     }
   }
   if (MODE != 0) {
