@@ -745,15 +745,10 @@ __device__ __forceinline__ void sb_rows(const CompVals& C, int d, int ref0, int 
   P2 pa[2] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
   const int nlow = refup - ref0, nup = ref1 - refup;
   const int nmax = nlow > nup ? nlow : nup;
-  // the refs of a lane's next step are loaded one step ahead, so that a
-  // step waits for one round trip (blocks and x) instead of two
-  int2 rln = t < nlow ? __ldcs(&C.sb_ref[ref0 + t]) : make_int2(0, 0);
-  int2 run = t < nup ? __ldcs(&C.sb_ref[refup + t]) : make_int2(0, 0);
   for (int j = t; j < nmax; j += S) {
     const bool hl = j < nlow, hu = j < nup;
-    const int2 rl = rln, ru = run;
-    rln = j + S < nlow ? __ldcs(&C.sb_ref[ref0 + j + S]) : make_int2(0, 0);
-    run = j + S < nup ? __ldcs(&C.sb_ref[refup + j + S]) : make_int2(0, 0);
+    const int2 rl = hl ? __ldcs(&C.sb_ref[ref0 + j]) : make_int2(0, 0);
+    const int2 ru = hu ? __ldcs(&C.sb_ref[refup + j]) : make_int2(0, 0);
     const int eql = rl.y & 0x7ffffff, dnl = hl ? (rl.y >> 27) & 7 : 0;
     const int equ = ru.y & 0x7ffffff, dnu = hu ? (ru.y >> 27) & 7 : 0;
     const int dl = hl ? d : 0;
@@ -806,8 +801,8 @@ __device__ __forceinline__ void sb_rows(const CompVals& C, int d, int ref0, int 
 // alpha = |xd . y| / beta^2.  S lanes per node (32 / S nodes per warp) in
 // the slot order; the row sums are reduced over the S lanes with the
 // transposed butterfly of k_spmv_cf.
-template <int MODE, int S, int MINB = 1>
-__global__ void __launch_bounds__(256, MINB)
+template <int MODE, int S>
+__global__ void __launch_bounds__(256)
     k_spmv_sb(CompVals C, const float2* __restrict__ xp, double* __restrict__ y,
               const double* __restrict__ xd, KrylovScalars* ks, double* partial,
               unsigned* counter) {
@@ -1993,16 +1988,6 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
     case kSbShape + 2: {
       static const int grid = resident_grid(k_spmv_sb<MODE, 32>);
       k_spmv_sb<MODE, 32><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
-      break;
-    }
-    case kSbShape + 3: {
-      static const int grid = resident_grid(k_spmv_sb<MODE, 16, 3>);
-      k_spmv_sb<MODE, 16, 3><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
-      break;
-    }
-    case kSbShape + 4: {
-      static const int grid = resident_grid(k_spmv_sb<MODE, 8, 3>);
-      k_spmv_sb<MODE, 8, 3><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
       break;
     }
     case 2: launch_cf<MODE, 8, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
