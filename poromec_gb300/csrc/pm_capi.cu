@@ -876,7 +876,7 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
     for (int c : pm::kCfShapes)
       if (u == c && !(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) &&
           !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0)) &&
-          !(c >= pm::kSbShape && c <= pm::kSbShape + 2 && (!h->P.sb_hi || h->ninst > 0))) {
+          !(c == pm::kSbShape && (!h->P.sb_hi || h->ninst > 0))) {
         h->shape = u;
         return PM_OK;
       }
@@ -893,7 +893,7 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
     // memory, and not for batches (it does not skip converged instances)
     if (!(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) &&
         !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0)) &&
-        !(c >= pm::kSbShape && c <= pm::kSbShape + 2 && (!h->P.sb_hi || h->ninst > 0)))
+        !(c == pm::kSbShape && (!h->P.sb_hi || h->ninst > 0)))
       cand.push_back(c);
   auto run = [&](int c) {
     const pm::CompVals C = h->P.comp(c);
@@ -943,13 +943,12 @@ int ensure_comp(Handle* h, cudaStream_t s) {
       PM_TRY(pm::build_sb_layout(h));
     }
   }
-  const bool sb = h->shape >= pm::kSbShape && h->shape <= pm::kSbShape + 2;
-  if (h->P.sb_hi && (h->shape == 0 || sb)) {
+  if (h->P.sb_hi && (h->shape == 0 || h->shape == pm::kSbShape)) {
     h->launches += 1;
     PM_CUDA(pm::split_blocks(h->P.view(), h->P.val, h->P.sb_build, h->P.sb_nblocks,
                              h->P.comp(h->shape), s));
   }
-  if (h->shape != pm::kCaShape && !sb) {
+  if (h->shape != pm::kCaShape && h->shape != pm::kSbShape) {
     h->launches += 1;
     PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
   }

@@ -177,8 +177,7 @@ struct CompVals {
               // arithmetic; 214: shape 14 held to 64 registers (4 CTAs per
               // SM), 312 / 314: shapes 112 / 114 held to 4 / 3 CTAs per SM;
               // kCaShape: the record kernel; kCsShape: the streamed record
-              // kernel; kSbShape, + 1, + 2: the symmetric block kernel with
-              // 8, 16, 32 lanes per node
+              // kernel; kSbShape: the symmetric block kernel
   // Symmetric block layout (shape kSbShape): the lower triangle and the
   // diagonal stored once, as node blocks.  The block of row node a and
   // column node b (eq0_b <= eq0_a) is d_a rows of four FP32 hi values
@@ -203,8 +202,7 @@ constexpr int kCsWarps = 8;                // consumer warps of the streamed ker
 constexpr int kCsNodes = 2 * kCsWarps;     // nodes per batch (one per half-warp)
 constexpr int kCsMaxStages = 4;
 constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,  104, 112,
-                              114, 124, 214, 312, 314, kCaShape, kCsShape, kSbShape,
-                              kSbShape + 1, kSbShape + 2};
+                              114, 124, 214, 312, 314, kCaShape, kCsShape, kSbShape};
 cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
 cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s);
 // Blocks of the symmetric block layout from the FP64 panels: build[i] =

@@ -399,6 +399,7 @@ int build_sb_layout(Handle* h) {
   std::vector<int32_t> eqnode(h->neq, -1);
   for (int k = 0; k < nact; ++k)
     for (int q = 0; q < h->h_d[k]; ++q) eqnode[h->h_eq0[k] + q] = k;
+  // visiting slots in equation order
   std::vector<int32_t> slot_node(nact);
   std::iota(slot_node.begin(), slot_node.end(), 0);
   std::sort(slot_node.begin(), slot_node.end(),
@@ -426,27 +427,6 @@ int build_sb_layout(Handle* h) {
         low_col[r] = j;
         ++r;
       }
-  }
-  // visiting slots: equation order (which keeps the two reads of a block
-  // close in time, for L2), and within runs of 1024 slots by free dofs and
-  // block count, so that the nodes sharing a warp run alike
-  {
-    std::vector<int32_t> nblk(nact, 0);
-    for (int k = 0; k < nact; ++k) {
-      const int32_t* c = h->h_cols.data() + h->h_col_off[k];
-      int runs = 0;
-      for (int j = 0; j < h->h_W[k]; ++j)
-        if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) ++runs;
-      nblk[k] = runs;
-    }
-    constexpr int kRun = 1024;
-    for (int i0 = 0; i0 < nact; i0 += kRun) {
-      const int i1 = std::min(nact, i0 + kRun);
-      std::stable_sort(slot_node.begin() + i0, slot_node.begin() + i1, [&](int a, int b) {
-        if (h->h_d[a] != h->h_d[b]) return h->h_d[a] > h->h_d[b];
-        return nblk[a] > nblk[b];
-      });
-    }
   }
   // block rows in the visiting order, so that a node's own blocks are
   // contiguous and the stream of them follows the visit

@@ -730,78 +730,49 @@ __device__ __forceinline__ float f4c(const float4& v, int c) {
   return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
 }
 
-// One node's rows on S lanes.  Step j of a lane takes its node's j-th own
-// lower or diagonal block (rows = the node's dofs, columns = the
-// neighbour's) and its j-th upper neighbour's stored block read transposed
-// (rows = the neighbour's dofs, columns = the node's own), with the loads of
-// both issued before their arithmetic.  Blocks are rows of four (zero
-// padding), the node's d <= 4 rows taken as four; both kinds accumulate into
-// the node's rows, two rows per packed f32x2 instruction.  Blocks are loaded
-// through L2 only (each is read by its two nodes); refs stream.
-template <int S>
-__device__ __forceinline__ void sb_rows(const CompVals& C, int d, int ref0, int refup,
-                                        int ref1, const float2* __restrict__ xp, int t,
-                                        F2 (&a)[4]) {
-  P2 pa[2] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};
-  const int nlow = refup - ref0, nup = ref1 - refup;
-  const int nmax = nlow > nup ? nlow : nup;
-  for (int j = t; j < nmax; j += S) {
-    const bool hl = j < nlow, hu = j < nup;
-    const int2 rl = hl ? __ldcs(&C.sb_ref[ref0 + j]) : make_int2(0, 0);
-    const int2 ru = hu ? __ldcs(&C.sb_ref[refup + j]) : make_int2(0, 0);
-    const int eql = rl.y & 0x7ffffff, dnl = hl ? (rl.y >> 27) & 7 : 0;
-    const int equ = ru.y & 0x7ffffff, dnu = hu ? (ru.y >> 27) & 7 : 0;
-    const int dl = hl ? d : 0;
-    float2 xl[4], xu[4];
-    float4 bl[4], bu[4];
-    int wl[4], wu[4];
+// One node's D rows: its own lower and diagonal blocks (rows = its dofs,
+// columns = the neighbour's), then the stored blocks of its upper
+// neighbours read transposed (rows = the neighbour's dofs, columns = its
+// own).  The lanes of the warp take the refs in turn; the x pairs of a
+// neighbour are its consecutive equations.  Blocks are loaded through L2
+// only (each is read by its two nodes); refs stream.
+template <int D>
+__device__ __forceinline__ void sb_rows(const CompVals& C, int ref0, int refup, int ref1,
+                                        const float2* __restrict__ xp, int lane, F2 (&a)[4]) {
+  for (int i = ref0 + lane; i < refup; i += 32) {
+    const int2 rf = __ldcs(&C.sb_ref[i]);
+    const int eq = rf.y & 0x7ffffff, dn = (rf.y >> 27) & 7;
+    float2 xv[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      xl[c] = c < dnl ? xp[eql + c] : make_float2(0.f, 0.f);
-      xu[c] = c < dnu ? xp[equ + c] : make_float2(0.f, 0.f);
-    }
+    for (int c = 0; c < 4; ++c) xv[c] = c < dn ? xp[eq + c] : make_float2(0.f, 0.f);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      bl[r] = r < dl ? __ldcg(&C.sb_hi[rl.x + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      wl[r] = r < dl ? __ldcg(&C.sb_lo[rl.x + r]) : 0;
-      bu[r] = r < dnu ? __ldcg(&C.sb_hi[ru.x + r]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      wu[r] = r < dnu ? __ldcg(&C.sb_lo[ru.x + r]) : 0;
-    }
-    // own block: rows (2k, 2k+1) of the node times the neighbour's x[c]
+    for (int r = 0; r < D; ++r) {
+      const float4 h = __ldcg(&C.sb_hi[rf.x + r]);
+      const int w = __ldcg(&C.sb_lo[rf.x + r]);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const f2x xh = pk2(xl[c].x, xl[c].x), nxh = pk2(-xl[c].x, -xl[c].x);
-      const f2x xo = pk2(xl[c].y, xl[c].y);
-#pragma unroll
-      for (int k = 0; k < 2; ++k)
-        p2_fma(pa[k], pk2(f4c(bl[2 * k], c), f4c(bl[2 * k + 1], c)),
-               p2_nqs(sb_q(wl[2 * k], c), sb_q(wl[2 * k + 1], c)), xh, nxh, xo);
-    }
-    // upper block transposed: the node's rows (2k, 2k+1) are columns of
-    // the neighbour's row r, times the neighbour's x[r]
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const f2x xh = pk2(xu[r].x, xu[r].x), nxh = pk2(-xu[r].x, -xu[r].x);
-      const f2x xo = pk2(xu[r].y, xu[r].y);
-#pragma unroll
-      for (int k = 0; k < 2; ++k)
-        p2_fma(pa[k], pk2(f4c(bu[r], 2 * k), f4c(bu[r], 2 * k + 1)),
-               p2_nqs(sb_q(wu[r], 2 * k), sb_q(wu[r], 2 * k + 1)), xh, nxh, xo);
+      for (int c = 0; c < 4; ++c) f2_fma(a[r], f4c(h, c), sb_q(w, c), xv[c].x, xv[c].y);
     }
   }
+  for (int i = refup + lane; i < ref1; i += 32) {
+    const int2 rf = __ldcs(&C.sb_ref[i]);
+    const int eq = rf.y & 0x7ffffff, dn = (rf.y >> 27) & 7;
 #pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    const float2 sn = up2(pa[k].sn), cn2 = up2(pa[k].cn), cp = up2(pa[k].cp);
-    a[2 * k] = F2{-sn.x, cp.x - cn2.x};
-    a[2 * k + 1] = F2{-sn.y, cp.y - cn2.y};
+    for (int r = 0; r < 4; ++r) {
+      if (r >= dn) break;
+      const float2 xr = xp[eq + r];
+      const float4 h = __ldcg(&C.sb_hi[rf.x + r]);
+      const int w = __ldcg(&C.sb_lo[rf.x + r]);
+#pragma unroll
+      for (int c = 0; c < D; ++c) f2_fma(a[c], f4c(h, c), sb_q(w, c), xr.x, xr.y);
+    }
   }
 }
 
 // MODE 0: y = A x.  MODE 1: PCG, alpha = d / (y . xd).  MODE 2: MINRES,
-// alpha = |xd . y| / beta^2.  S lanes per node (32 / S nodes per warp) in
-// the slot order; the row sums are reduced over the S lanes with the
-// transposed butterfly of k_spmv_cf.
-template <int MODE, int S>
+// alpha = |xd . y| / beta^2.  One warp per node in equation order; the D
+// row sums are reduced over the 32 lanes with the transposed butterfly of
+// k_spmv_cf.
+template <int MODE>
 __global__ void __launch_bounds__(256)
     k_spmv_sb(CompVals C, const float2* __restrict__ xp, double* __restrict__ y,
               const double* __restrict__ xd, KrylovScalars* ks, double* partial,
@@ -809,32 +780,30 @@ __global__ void __launch_bounds__(256)
   if (MODE != 0)
     if (krylov_skip(ks, true)) return;
   const int lane = threadIdx.x & 31;
-  const int t = lane & (S - 1);
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
-  constexpr int kNodesPerWarp = 32 / S;
   double dsum = 0.0;
-  for (int base = warp * kNodesPerWarp; base < C.sb_nslots; base += nwarp * kNodesPerWarp) {
-    const int sl = base + lane / S;
-    int4 nd = make_int4(0, 0, 0, 0);
-    int ref1 = 0;
-    if (sl < C.sb_nslots) {
-      nd = C.sb_node[sl];
-      ref1 = C.sb_node[sl + 1].z;
+  for (int sl = warp; sl < C.sb_nslots; sl += nwarp) {
+    const int4 nd = C.sb_node[sl];
+    const int ref1 = C.sb_node[sl + 1].z;
+    F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    switch (nd.y) {
+      case 4: sb_rows<4>(C, nd.z, nd.w, ref1, xp, lane, a); break;
+      case 3: sb_rows<3>(C, nd.z, nd.w, ref1, xp, lane, a); break;
+      case 2: sb_rows<2>(C, nd.z, nd.w, ref1, xp, lane, a); break;
+      default: sb_rows<1>(C, nd.z, nd.w, ref1, xp, lane, a); break;
     }
-    F2 a[4];
-    sb_rows<S>(C, nd.y, nd.z, nd.w, sl < C.sb_nslots ? ref1 : nd.w, xp, t, a);
-    constexpr int o1 = S / 2, o2 = S / 4;
-    const bool h1 = (t & o1) != 0, h2 = (t & o2) != 0;
+    constexpr int o1 = 16, o2 = 8;
+    const bool h1 = (lane & o1) != 0, h2 = (lane & o2) != 0;
     F2 k0 = h1 ? a[2] : a[0], k1 = h1 ? a[3] : a[1];
     k0 = f2_add(k0, f2_shfl(h1 ? a[0] : a[2], o1));
     k1 = f2_add(k1, f2_shfl(h1 ? a[1] : a[3], o1));
     F2 k = h2 ? k1 : k0;
     k = f2_add(k, f2_shfl(h2 ? k0 : k1, o2));
 #pragma unroll
-    for (int o = S / 8; o > 0; o >>= 1) k = f2_add(k, f2_shfl(k, o));
+    for (int o = 4; o > 0; o >>= 1) k = f2_add(k, f2_shfl(k, o));
     const int r = (h1 ? 2 : 0) + (h2 ? 1 : 0);
-    if ((t & (o2 - 1)) == 0 && r < nd.y) {
+    if ((lane & (o2 - 1)) == 0 && r < nd.y) {
       const double v = double(k.s) + double(k.c);
       y[nd.x + r] = v;
       if (MODE != 0) dsum += v * xd[nd.x + r];
@@ -1976,18 +1945,8 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
                                                                            partial, counter);
       break;
     case kSbShape: {
-      static const int grid = resident_grid(k_spmv_sb<MODE, 8>);
-      k_spmv_sb<MODE, 8><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
-      break;
-    }
-    case kSbShape + 1: {
-      static const int grid = resident_grid(k_spmv_sb<MODE, 16>);
-      k_spmv_sb<MODE, 16><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
-      break;
-    }
-    case kSbShape + 2: {
-      static const int grid = resident_grid(k_spmv_sb<MODE, 32>);
-      k_spmv_sb<MODE, 32><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
+      static const int grid = resident_grid(k_spmv_sb<MODE>);
+      k_spmv_sb<MODE><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
       break;
     }
     case 2: launch_cf<MODE, 8, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
