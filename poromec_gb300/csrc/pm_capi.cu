@@ -875,8 +875,7 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
     const int u = std::atoi(env);
     for (int c : pm::kCfShapes)
       if (u == c && !(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) &&
-          !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0)) &&
-          !(c == pm::kSbShape && (!h->P.sb_hi || h->ninst > 0))) {
+          !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0))) {
         h->shape = u;
         return PM_OK;
       }
@@ -892,8 +891,7 @@ int tune_spmvc(Handle* h, cudaStream_t s) {
     // the record kernel: only where two records per warp fit in shared
     // memory, and not for batches (it does not skip converged instances)
     if (!(c == pm::kCaShape && (h->P.ca_warps == 0 || h->ninst > 0)) &&
-        !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0)) &&
-        !(c == pm::kSbShape && (!h->P.sb_hi || h->ninst > 0)))
+        !(c == pm::kCsShape && (h->P.cs_nstage == 0 || h->ninst > 0)))
       cand.push_back(c);
   auto run = [&](int c) {
     const pm::CompVals C = h->P.comp(c);
@@ -938,17 +936,9 @@ int ensure_comp(Handle* h, cudaStream_t s) {
   if (!h->P.valh) {
     PM_CUDA(cudaMalloc(&h->P.valh, sizeof(float) * (size_t)h->P.nnz));
     PM_CUDA(cudaMalloc(&h->P.vall, sizeof(int8_t) * (size_t)h->P.nnz));
-    if (h->ninst == 0) {  // batches use neither records nor symmetric blocks
-      PM_TRY(pm::build_rec_layout(h));
-      PM_TRY(pm::build_sb_layout(h));
-    }
+    if (h->ninst == 0) PM_TRY(pm::build_rec_layout(h));  // batches do not use records
   }
-  if (h->P.sb_hi && (h->shape == 0 || h->shape == pm::kSbShape)) {
-    h->launches += 1;
-    PM_CUDA(pm::split_blocks(h->P.view(), h->P.val, h->P.sb_build, h->P.sb_nblocks,
-                             h->P.comp(h->shape), s));
-  }
-  if (h->shape != pm::kCaShape && h->shape != pm::kSbShape) {
+  if (h->shape != pm::kCaShape) {
     h->launches += 1;
     PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
   }
@@ -1272,7 +1262,7 @@ void free_all(Handle* h) {
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
                   P.val32, P.valh, P.vall, P.rec, P.rec_off, P.node_val_off, P.node_W,
                   P.order, P.cs_desc, P.cs_batch_slot, P.cs_batch_off, P.cs_batch_bytes,
-                  P.cs_cta_batch, P.fault, P.sb_hi, P.sb_lo, P.sb_ref, P.sb_node, P.sb_build};
+                  P.cs_cta_batch, P.fault};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})

@@ -57,14 +57,6 @@ struct Panels {
   int64_t* cs_batch_off = nullptr;
   int cs_grid = 0, cs_nstage = 0, cs_stage_bytes = 0;
   int* fault = nullptr;
-  // symmetric block layout (CompVals, shape kSbShape) and its build list
-  float4* sb_hi = nullptr;
-  int* sb_lo = nullptr;
-  int2* sb_ref = nullptr;
-  int4* sb_node = nullptr;
-  int4* sb_build = nullptr;
-  int64_t sb_nblocks = 0;
-  int sb_nslots = 0;
   // batches: instance of each active node, done flag of each instance
   int32_t* node_inst = nullptr;
   int* inst_done = nullptr;
@@ -82,8 +74,7 @@ struct Panels {
     return CompVals{valh,          vall,          rec,          rec_off,        rec_max,
                     ca_warps,      ca_grid,       cs_desc,      cs_batch_slot,  cs_batch_off,
                     cs_batch_bytes, cs_cta_batch, cs_grid,      cs_nstage,      cs_stage_bytes,
-                    fault,         shape,         sb_hi,        sb_lo,          sb_ref,
-                    sb_node,       sb_nslots};
+                    fault,         shape};
   }
 };
 
@@ -232,7 +223,5 @@ struct Handle {
 int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
                     const int32_t* fnno, const double* x, const int32_t* num);
 int build_rec_layout(Handle* h);
-// the symmetric block layout of the compensated operator (single meshes)
-int build_sb_layout(Handle* h);
 
 }  // namespace pm

@@ -177,38 +177,16 @@ struct CompVals {
               // arithmetic; 214: shape 14 held to 64 registers (4 CTAs per
               // SM), 312 / 314: shapes 112 / 114 held to 4 / 3 CTAs per SM;
               // kCaShape: the record kernel; kCsShape: the streamed record
-              // kernel; kSbShape: the symmetric block kernel
-  // Symmetric block layout (shape kSbShape): the lower triangle and the
-  // diagonal stored once, as node blocks.  The block of row node a and
-  // column node b (eq0_b <= eq0_a) is d_a rows of four FP32 hi values
-  // (b's d_b columns, zero-padded) in sb_hi and four int8 corrections per
-  // row packed in one int in sb_lo.  Nodes are visited in equation order,
-  // one warp each; slot s has sb_node[s] = {eq0, d, first ref, first upper
-  // ref} (sb_node[nslots].z = end of its refs), and each ref is
-  // {first block row, eq0_nb | d_nb << 27 | transposed << 30}: a lower or
-  // diagonal block of the node itself (rows = the node's dofs) or an upper
-  // one, the stored block of the neighbour read transposed.  Every block is
-  // read by its two nodes, the second read mostly from L2 (equation order
-  // keeps neighbours close in time); rows are summed by one warp in a fixed
-  // order, so the product is deterministic without atomics.
-  const float4* sb_hi;
-  const int* sb_lo;
-  const int2* sb_ref;
-  const int4* sb_node;
-  int sb_nslots;
+              // kernel
 };
-constexpr int kCaShape = 90, kCsShape = 91, kSbShape = 95;
+constexpr int kCaShape = 90, kCsShape = 91;
 constexpr int kCsWarps = 8;                // consumer warps of the streamed kernel
 constexpr int kCsNodes = 2 * kCsWarps;     // nodes per batch (one per half-warp)
 constexpr int kCsMaxStages = 4;
-constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,  104, 112,
-                              114, 124, 214, 312, 314, kCaShape, kCsShape, kSbShape};
+constexpr int kCfShapes[] = {1,   2,   4,   11,  12,  14,  21,  22,  24,
+                              104, 112, 114, 124, 214, 312, 314, kCaShape, kCsShape};
 cudaError_t split_values(int64_t n, const double* v, float* hi, int8_t* lo, cudaStream_t s);
 cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaStream_t s);
-// Blocks of the symmetric block layout from the FP64 panels: build[i] =
-// {active node k, first panel column of the block, first block row, d_b}.
-cudaError_t split_blocks(const PanelView& P, const double* v, const int4* build,
-                         int64_t nblocks, CompVals C, cudaStream_t s);
 // Dynamic shared memory of the record kernel for a given record size and
 // warp count, and the set-up of its launch attributes (once per process).
 int ca_smem_bytes(int rec_max, int warps);

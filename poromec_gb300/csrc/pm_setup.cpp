@@ -386,124 +386,4 @@ int build_rec_layout(Handle* h) {
   return PM_OK;
 }
 
-// Symmetric block layout of the compensated operator (CompVals, shape
-// kSbShape).  From the panels: each panel's columns are runs of its
-// neighbours' consecutive equations; the runs of equations up to the node's
-// own are its lower and diagonal blocks, stored once under the node (rows
-// assigned in equation order); every node refers to its own lower blocks
-// and, transposed, to the lower blocks of its upper neighbours.
-int build_sb_layout(Handle* h) {
-  Panels& P = h->P;
-  const int nact = P.nact;
-  if (nact == 0 || h->neq >= (1 << 27)) return PM_OK;  // the ref encoding needs eq0 < 2^27
-  std::vector<int32_t> eqnode(h->neq, -1);
-  for (int k = 0; k < nact; ++k)
-    for (int q = 0; q < h->h_d[k]; ++q) eqnode[h->h_eq0[k] + q] = k;
-  // visiting slots in equation order
-  std::vector<int32_t> slot_node(nact);
-  std::iota(slot_node.begin(), slot_node.end(), 0);
-  std::sort(slot_node.begin(), slot_node.end(),
-            [&](int a, int b) { return h->h_eq0[a] < h->h_eq0[b]; });
-  // lower runs of every node: (neighbour, first panel column), stored rows
-  std::vector<int64_t> low_ptr(nact + 1, 0);
-  for (int k = 0; k < nact; ++k) {
-    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
-    const int n = h->h_low[k] + h->h_d[k];
-    int runs = 0;
-    for (int j = 0; j < n; ++j)
-      if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) ++runs;
-    low_ptr[k + 1] = runs;
-  }
-  for (int k = 0; k < nact; ++k) low_ptr[k + 1] += low_ptr[k];
-  const int64_t nblocks = low_ptr[nact];
-  std::vector<int32_t> low_nb(nblocks), low_col(nblocks), low_row(nblocks);
-  for (int k = 0; k < nact; ++k) {
-    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
-    const int n = h->h_low[k] + h->h_d[k];
-    int64_t r = low_ptr[k];
-    for (int j = 0; j < n; ++j)
-      if (j == 0 || eqnode[c[j]] != eqnode[c[j - 1]]) {
-        low_nb[r] = eqnode[c[j]];
-        low_col[r] = j;
-        ++r;
-      }
-  }
-  // block rows in the visiting order, so that a node's own blocks are
-  // contiguous and the stream of them follows the visit
-  int64_t rows = 0;
-  for (int i = 0; i < nact; ++i) {
-    const int k = slot_node[i];
-    for (int64_t r = low_ptr[k]; r < low_ptr[k + 1]; ++r) {
-      low_row[r] = (int32_t)rows;
-      rows += h->h_d[k];
-      if (rows >= (int64_t)1 << 31) return PM_OK;  // row indices are int32
-    }
-  }
-  std::vector<int4> build(nblocks);
-  for (int k = 0; k < nact; ++k)
-    for (int64_t r = low_ptr[k]; r < low_ptr[k + 1]; ++r)
-      build[r] = make_int4(k, low_col[r], low_row[r], h->h_d[low_nb[r]]);
-  // refs per slot: own lower blocks, then the upper neighbours' blocks
-  std::vector<int4> node(nact + 1);
-  std::vector<int64_t> ref_ptr(nact + 1, 0);
-  for (int i = 0; i < nact; ++i) {
-    const int k = slot_node[i];
-    int upper = 0;
-    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
-    for (int j = h->h_low[k] + h->h_d[k]; j < h->h_W[k]; ++j)
-      if (eqnode[c[j]] != eqnode[c[j - 1]]) ++upper;
-    ref_ptr[i + 1] = ref_ptr[i] + (low_ptr[k + 1] - low_ptr[k]) + upper;
-  }
-  if (ref_ptr[nact] >= (int64_t)1 << 31) return PM_OK;
-  std::vector<int2> ref(ref_ptr[nact]);
-  auto enc = [&](int m, int transposed) {
-    return (int)((unsigned)h->h_eq0[m] | ((unsigned)h->h_d[m] << 27) |
-                 ((unsigned)transposed << 30));
-  };
-  int bad = 0;
-#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : bad)
-  for (int i = 0; i < nact; ++i) {
-    const int k = slot_node[i];
-    int64_t o = ref_ptr[i];
-    for (int64_t r = low_ptr[k]; r < low_ptr[k + 1]; ++r)
-      ref[o++] = make_int2(low_row[r], enc(low_nb[r], 0));
-    const int64_t up = o;
-    const int32_t* c = h->h_cols.data() + h->h_col_off[k];
-    for (int j = h->h_low[k] + h->h_d[k]; j < h->h_W[k]; ++j) {
-      if (eqnode[c[j]] == eqnode[c[j - 1]]) continue;
-      const int m = eqnode[c[j]];
-      // k's block in m's lower runs (sorted by equation)
-      int64_t lo = low_ptr[m], hi = low_ptr[m + 1];
-      while (lo < hi) {
-        const int64_t mid = (lo + hi) / 2;
-        if (h->h_eq0[low_nb[mid]] < h->h_eq0[k]) lo = mid + 1;
-        else hi = mid;
-      }
-      if (lo >= low_ptr[m + 1] || low_nb[lo] != k) {
-        ++bad;
-        continue;
-      }
-      ref[o++] = make_int2(low_row[lo], enc(m, 1));
-    }
-    node[i] = make_int4(h->h_eq0[k], h->h_d[k], (int)ref_ptr[i], (int)up);
-  }
-  if (bad) {  // an unsymmetric pattern: leave the layout out
-    if (getenv("PM_DEBUG")) fprintf(stderr, "symmetric block layout: %d unmatched blocks\n", bad);
-    return PM_OK;
-  }
-  node[nact] = make_int4(0, 0, (int)ref_ptr[nact], (int)ref_ptr[nact]);
-  int st;
-  if ((st = upload<float4>(h, &P.sb_hi, nullptr, (size_t)rows))) return st;
-  if ((st = upload<int>(h, &P.sb_lo, nullptr, (size_t)rows))) return st;
-  if ((st = upload(h, &P.sb_ref, ref.data(), ref.size()))) return st;
-  if ((st = upload(h, &P.sb_node, node.data(), node.size()))) return st;
-  if ((st = upload(h, &P.sb_build, build.data(), build.size()))) return st;
-  P.sb_nblocks = nblocks;
-  P.sb_nslots = nact;
-  if (getenv("PM_DEBUG"))
-    fprintf(stderr, "symmetric block layout: %lld blocks, %lld rows, %lld refs\n",
-            (long long)nblocks, (long long)rows, (long long)ref_ptr[nact]);
-  return PM_OK;
-}
-
 }  // namespace pm

@@ -690,138 +690,6 @@ __global__ void __launch_bounds__(256, MINB)
   }
 }
 
-// ---- symmetric block kernel (shape kSbShape, layout in CompVals) ------------
-// The blocks of the lower triangle and the diagonal from the FP64 panels:
-// build[i] = {active node k, first panel column c0, first block row, d_b}:
-// rows q < d_k of k's panel, columns c0 .. c0 + d_b - 1, each value split as
-// k_split_values does, the row padded with zeros to four columns.
-__global__ void __launch_bounds__(256)
-    k_sb_split(PanelView P, const double* __restrict__ v, const int4* __restrict__ build,
-               int64_t nblocks, float4* __restrict__ hi, int* __restrict__ lo) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nblocks;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int4 b = build[i];
-    const int W = P.W[b.x], da = P.d[b.x];
-    const double* row0 = v + P.val_off[b.x] + b.y;
-    for (int q = 0; q < da; ++q) {
-      float h[4] = {0.f, 0.f, 0.f, 0.f};
-      unsigned packed = 0u;
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (c < b.w) {
-          const double a = row0[(int64_t)q * W + c];
-          const float hh = float(a);
-          float qq = 0.f;
-          if (hh != 0.f && isfinite(hh)) qq = rintf(float(a - double(hh)) / hh * 2147483648.0f);
-          const int qi = (int)fminf(fmaxf(qq, -127.f), 127.f);
-          h[c] = hh;
-          packed |= (unsigned)(qi & 0xff) << (8 * c);
-        }
-      hi[b.z + q] = make_float4(h[0], h[1], h[2], h[3]);
-      lo[b.z + q] = (int)packed;
-    }
-  }
-}
-
-// byte c of a packed word of four int8 corrections, sign-extended
-__device__ __forceinline__ int sb_q(int w, int c) { return (w << (24 - 8 * c)) >> 24; }
-
-__device__ __forceinline__ float f4c(const float4& v, int c) {
-  return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
-}
-
-// One node's D rows: its own lower and diagonal blocks (rows = its dofs,
-// columns = the neighbour's), then the stored blocks of its upper
-// neighbours read transposed (rows = the neighbour's dofs, columns = its
-// own).  The lanes of the warp take the refs in turn; the x pairs of a
-// neighbour are its consecutive equations.  Blocks are loaded through L2
-// only (each is read by its two nodes); refs stream.
-template <int D>
-__device__ __forceinline__ void sb_rows(const CompVals& C, int ref0, int refup, int ref1,
-                                        const float2* __restrict__ xp, int lane, F2 (&a)[4]) {
-  for (int i = ref0 + lane; i < refup; i += 32) {
-    const int2 rf = __ldcs(&C.sb_ref[i]);
-    const int eq = rf.y & 0x7ffffff, dn = (rf.y >> 27) & 7;
-    float2 xv[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) xv[c] = c < dn ? xp[eq + c] : make_float2(0.f, 0.f);
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-      const float4 h = __ldcg(&C.sb_hi[rf.x + r]);
-      const int w = __ldcg(&C.sb_lo[rf.x + r]);
-#pragma unroll
-      for (int c = 0; c < 4; ++c) f2_fma(a[r], f4c(h, c), sb_q(w, c), xv[c].x, xv[c].y);
-    }
-  }
-  for (int i = refup + lane; i < ref1; i += 32) {
-    const int2 rf = __ldcs(&C.sb_ref[i]);
-    const int eq = rf.y & 0x7ffffff, dn = (rf.y >> 27) & 7;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      if (r >= dn) break;
-      const float2 xr = xp[eq + r];
-      const float4 h = __ldcg(&C.sb_hi[rf.x + r]);
-      const int w = __ldcg(&C.sb_lo[rf.x + r]);
-#pragma unroll
-      for (int c = 0; c < D; ++c) f2_fma(a[c], f4c(h, c), sb_q(w, c), xr.x, xr.y);
-    }
-  }
-}
-
-// MODE 0: y = A x.  MODE 1: PCG, alpha = d / (y . xd).  MODE 2: MINRES,
-// alpha = |xd . y| / beta^2.  One warp per node in equation order; the D
-// row sums are reduced over the 32 lanes with the transposed butterfly of
-// k_spmv_cf.
-template <int MODE>
-__global__ void __launch_bounds__(256)
-    k_spmv_sb(CompVals C, const float2* __restrict__ xp, double* __restrict__ y,
-              const double* __restrict__ xd, KrylovScalars* ks, double* partial,
-              unsigned* counter) {
-  if (MODE != 0)
-    if (krylov_skip(ks, true)) return;
-  const int lane = threadIdx.x & 31;
-  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
-  double dsum = 0.0;
-  for (int sl = warp; sl < C.sb_nslots; sl += nwarp) {
-    const int4 nd = C.sb_node[sl];
-    const int ref1 = C.sb_node[sl + 1].z;
-    F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    switch (nd.y) {
-      case 4: sb_rows<4>(C, nd.z, nd.w, ref1, xp, lane, a); break;
-      case 3: sb_rows<3>(C, nd.z, nd.w, ref1, xp, lane, a); break;
-      case 2: sb_rows<2>(C, nd.z, nd.w, ref1, xp, lane, a); break;
-      default: sb_rows<1>(C, nd.z, nd.w, ref1, xp, lane, a); break;
-    }
-    constexpr int o1 = 16, o2 = 8;
-    const bool h1 = (lane & o1) != 0, h2 = (lane & o2) != 0;
-    F2 k0 = h1 ? a[2] : a[0], k1 = h1 ? a[3] : a[1];
-    k0 = f2_add(k0, f2_shfl(h1 ? a[0] : a[2], o1));
-    k1 = f2_add(k1, f2_shfl(h1 ? a[1] : a[3], o1));
-    F2 k = h2 ? k1 : k0;
-    k = f2_add(k, f2_shfl(h2 ? k0 : k1, o2));
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) k = f2_add(k, f2_shfl(k, o));
-    const int r = (h1 ? 2 : 0) + (h2 ? 1 : 0);
-    if ((lane & (o2 - 1)) == 0 && r < nd.y) {
-      const double v = double(k.s) + double(k.c);
-      y[nd.x + r] = v;
-      if (MODE != 0) dsum += v * xd[nd.x + r];
-    }
-  }
-  if (MODE != 0) {
-    double in[1] = {dsum}, tot[1];
-    if (grid_reduce<1>(in, partial, counter, tot) && threadIdx.x == 0) {
-      if (MODE == 1) {
-        ks->pq = tot[0];
-        ks->alpha = ks->d / tot[0];
-      } else {
-        ks->alpha = fabs(tot[0]) * (1.0 / (ks->beta * ks->beta));
-      }
-    }
-  }
-}
-
 // ---- record kernel: node records streamed into shared memory by cp.async ----
 // Each warp takes nodes gw, gw + nw, ... of the visiting order (gw its global
 // warp index, nw the warps of the grid) and keeps two record buffers in
@@ -1781,16 +1649,6 @@ cudaError_t split_records(const PanelView& P, const double* v, CompVals C, cudaS
   return cudaGetLastError();
 }
 
-cudaError_t split_blocks(const PanelView& P, const double* v, const int4* build,
-                         int64_t nblocks, CompVals C, cudaStream_t s) {
-  int64_t g = (nblocks + 255) / 256;
-  if (g > 8 * kRedBlocks) g = 8 * kRedBlocks;
-  if (g < 1) g = 1;
-  k_sb_split<<<(int)g, 256, 0, s>>>(P, v, build, nblocks, const_cast<float4*>(C.sb_hi),
-                                    const_cast<int*>(C.sb_lo));
-  return cudaGetLastError();
-}
-
 cudaError_t split_pair(int n, const double* v, float2* pr, cudaStream_t s) {
   k_split_pair<<<vec_grid(n), 256, 0, s>>>(n, v, pr);
   return cudaGetLastError();
@@ -1944,11 +1802,6 @@ void launch_spmv_cf(const PanelView& P, CompVals C, const float2* xp, double* y,
                         cs_smem_bytes(C.cs_nstage, C.cs_stage_bytes), s>>>(P, C, xp, y, xd, ks,
                                                                            partial, counter);
       break;
-    case kSbShape: {
-      static const int grid = resident_grid(k_spmv_sb<MODE>);
-      k_spmv_sb<MODE><<<grid, 256, 0, s>>>(C, xp, y, xd, ks, partial, counter);
-      break;
-    }
     case 2: launch_cf<MODE, 8, 2>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 4: launch_cf<MODE, 8, 4>(P, C, xp, y, xd, ks, partial, counter, s); break;
     case 11: launch_cf<MODE, 16, 1>(P, C, xp, y, xd, ks, partial, counter, s); break;

@@ -379,7 +379,7 @@ def _abs_product(m, x):
     return np.abs(ad) * ax + L @ ax + L.T @ ax
 
 
-@pytest.mark.parametrize("shape", [None, 1, 14, 24, 90, 91, 95, 104, 112, 114, 124, 214, 312, 314])
+@pytest.mark.parametrize("shape", [None, 1, 14, 24, 90, 91, 104, 112, 114, 124, 214, 312, 314])
 def test_compensated_spmv_rounding_bound(problems, shape, monkeypatch):
     """PM_FP32C_REFINE operator: values FP32 + an int8 relative correction
     (within 2^-32 |v|), x as an FP32 pair (2^-48), compensated sums: each row
@@ -401,7 +401,7 @@ def test_compensated_spmv_rounding_bound(problems, shape, monkeypatch):
             assert m.tune_spmv() == shape
 
 
-@pytest.mark.parametrize("shape", [None, 14, 91, 95, 104, 114, 124, 214, 314])
+@pytest.mark.parametrize("shape", [None, 14, 91, 104, 114, 124, 214, 314])
 # MINRES cases: the jittered tetra mesh and the cube; on the golden tetra
 # column MINRES itself stalls (the reference's FP64 MINRES and the oracle
 # need ~8e5 iterations there), which says nothing about the operator
