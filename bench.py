@@ -143,7 +143,7 @@ def relaunch_ranks(args):
         port = s.getsockname()[1]
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
            "--nproc-per-node", str(args.gpus), "--master-addr", "127.0.0.1",
-           "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+           "--master-port", str(port), "--", os.path.abspath(__file__)] + sys.argv[1:]
     return subprocess.call(cmd)
 
 

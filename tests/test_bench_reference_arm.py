@@ -50,3 +50,20 @@ def test_reference_arm_needs_a_measured_iteration_count():
                        text=True, cwd=ROOT, timeout=600)
     assert r.returncode != 0
     assert "--ref-iters" in r.stderr
+
+
+def test_gpus_n_starts_its_own_ranks():
+    """`bench.py --gpus 2` outside torchrun starts two local ranks itself
+    (torch.distributed.run on 127.0.0.1); under them the reference arm runs
+    on rank 0 only and reports n_gpus 2.  CPU only."""
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--gpus", "2", "--steps", "1", "--warmup", "0", "--n", "6",
+                        "--ref-iters", "50"], capture_output=True, text=True, cwd=ROOT,
+                       timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2
