@@ -256,6 +256,77 @@ int capture(Handle* h, cudaGraphExec_t* exec, Body body) {
   return PM_OK;
 }
 
+// A whole FP64 PCG solve as one graph: a conditional while node whose body
+// is kGraphIters iterations followed by loop_next, which keeps the loop going
+// while the solve runs (and bounds its trips by maxit), so the host waits
+// once per solve instead of once per kGraphIters iterations.  Built on the
+// first solve; if the driver refuses any part, the solve keeps the polled
+// graphs (run_graph).
+int build_pcg_loop(Handle* h) {
+  if (h->pcg_loop || h->pcg_loop_failed) return PM_OK;
+  if (std::getenv("PM_POLLED_GRAPHS")) {  // the host-polled graphs instead
+    h->pcg_loop_failed = true;
+    return PM_OK;
+  }
+  const pm::PanelView P = h->P.view();
+  pm::KrylovVecs& V = h->D.kv;
+  const int n = h->neq;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+  cudaGraphConditionalHandle cond{};
+  cudaGraphNodeParams np{};
+  cudaGraphNode_t node{};
+  if (ok && !h->D.trips) ok = cudaMalloc(&h->D.trips, sizeof(int)) == cudaSuccess;
+  // the handle is 0 at every launch; the start kernel sets it to 1
+  if (ok) ok = cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault) ==
+               cudaSuccess;
+  cudaGraphNode_t start{};
+  if (ok) {
+    ok = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      const cudaError_t le = pm::loop_start(h->D.trips, cond, h->stream);
+      cudaGraph_t out = nullptr;
+      ok = cudaStreamEndCapture(h->stream, &out) == cudaSuccess && le == cudaSuccess;
+    }
+    size_t nn = 1;
+    if (ok) ok = cudaGraphGetNodes(g, &start, &nn) == cudaSuccess && nn == 1;
+  }
+  if (ok) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, g, &start, nullptr, 1, &np) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      cudaError_t be = cudaSuccess;
+      for (int k = 0; k < kGraphIters && be == cudaSuccess; ++k)
+        be = pm::pcg_iteration(P, h->P.val, n, h->D.m, V, h->D.ks, h->D.partial, h->D.counter,
+                               h->stream);
+      if (be == cudaSuccess) be = pm::loop_next(h->D.ks, h->D.trips, cond, kGraphIters, h->stream);
+      cudaGraph_t out = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(h->stream, &out);
+      ok = be == cudaSuccess && ee == cudaSuccess;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    cudaGetLastError();  // the refusal is not this solve's error
+    h->pcg_loop_failed = true;
+    if (h->debug) fprintf(stderr, "device-side PCG loop unavailable: polled graphs\n");
+    return PM_OK;
+  }
+  h->pcg_loop = exec;
+  return PM_OK;
+}
+
 // Runs graphs of kGraphIters iterations until the solve's flag is set.
 int run_graph(Handle* h, cudaGraphExec_t g, pm::KrylovScalars* ks) {
   for (;;) {
@@ -476,7 +547,23 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       PM_CUDA(pm::pcg_init(n, d_b, h->D.m, V, h->D.ks, tol, maxit, h->D.partial, h->D.counter,
                            h->stream));
     if (!comp) {
-      PM_TRY(run_graph(h, *g, &ks));
+      PM_TRY(build_pcg_loop(h));
+      if (h->pcg_loop) {
+        PM_CUDA(cudaGraphLaunch(h->pcg_loop, h->stream));
+        PM_TRY(read_scalars(h, &ks));
+        h->launches += 1 + (3 * kGraphIters + 1) * ((ks.iter + kGraphIters - 1) / kGraphIters);
+        if (ks.conv_flag == 0) {
+          // the loop ended without the solve's flag (its condition was not
+          // honoured): finish with the polled graphs from where it stopped,
+          // and use those from now on
+          h->pcg_loop_failed = true;
+          cudaGraphExecDestroy(h->pcg_loop);
+          h->pcg_loop = nullptr;
+          PM_TRY(run_graph(h, *g, &ks));
+        }
+      } else {
+        PM_TRY(run_graph(h, *g, &ks));
+      }
     } else {
       // The compensated products (2^-32 per value) make the recursive
       // residual drift from b - A x.  Every time it has fallen by a factor
@@ -1268,6 +1355,8 @@ void free_all(Handle* h) {
   for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})
     if (p) cudaFree(p);
   if (h->pcg_graph) cudaGraphExecDestroy(h->pcg_graph);
+  if (h->pcg_loop) cudaGraphExecDestroy(h->pcg_loop);
+  if (h->D.trips) cudaFree(h->D.trips);
   if (h->pcgm_graph) cudaGraphExecDestroy(h->pcgm_graph);
   if (h->minres_graph) cudaGraphExecDestroy(h->minres_graph);
   if (h->pcgc_graph) cudaGraphExecDestroy(h->pcgc_graph);

@@ -154,6 +154,7 @@ struct Dev {
   unsigned* counter = nullptr;
   double* norms = nullptr;
   int* err = nullptr;
+  int* trips = nullptr;  // trips of the device-side solve loop (pcg_loop)
 };
 
 struct Handle {
@@ -214,6 +215,11 @@ struct Handle {
   cudaGraphExec_t bpcg_graph = nullptr, bpcgc_graph = nullptr;
   cudaGraphExec_t sqmr_graph = nullptr;
   cudaGraphExec_t sqmrc_graph = nullptr;
+  // a whole FP64 PCG solve in one graph: a conditional while node around
+  // kGraphIters iterations (built on the first solve; not used if the
+  // driver cannot build it)
+  cudaGraphExec_t pcg_loop = nullptr;
+  bool pcg_loop_failed = false;
   double timers[8] = {0};
   int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;

@@ -207,6 +207,15 @@ cudaError_t pcgc_init(int n, const double* b, const double* m, KrylovVecs& V,
 cudaError_t pcgc_iteration(const PanelView& P, CompVals C, int n, const double* m,
                            KrylovVecs& V, KrylovVecs32& V32, KrylovScalars* ks,
                            double* partial, unsigned* counter, cudaStream_t s);
+// A device-side solve loop: loop_start, before the conditional while node,
+// resets *trips and opens the loop (the handle's launch value is 0, so a
+// loop whose condition is never set does not run); loop_next, the last
+// kernel of the body, keeps it going while the solve has neither converged
+// nor stopped (ks->conv_flag == 0), at most ks->maxit / iters_per_trip + 4
+// trips.
+cudaError_t loop_start(int* trips, cudaGraphConditionalHandle cond, cudaStream_t s);
+cudaError_t loop_next(const KrylovScalars* ks, int* trips, cudaGraphConditionalHandle cond,
+                      int iters_per_trip, cudaStream_t s);
 // residual replacement of the compensated PCG: r = b - q (q = A x in FP64),
 // z = m r, d = (r, z), flags re-decided; x and p kept
 cudaError_t pcgc_replace(int n, const double* b, const double* q, const double* m,

@@ -1875,6 +1875,35 @@ cudaError_t minresc_iteration(const PanelView& P, CompVals C, int n, const doubl
   return cudaGetLastError();
 }
 
+namespace {
+__global__ void k_loop_start(int* trips, cudaGraphConditionalHandle cond) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *trips = 0;
+    cudaGraphSetConditional(cond, 1u);
+  }
+}
+
+__global__ void k_loop_next(const KrylovScalars* ks, int* trips,
+                            cudaGraphConditionalHandle cond, int iters_per_trip) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int t = ++*trips;
+    const int cap = ks->maxit / iters_per_trip + 4;
+    cudaGraphSetConditional(cond, (ks->conv_flag == 0 && t < cap) ? 1u : 0u);
+  }
+}
+}  // namespace
+
+cudaError_t loop_start(int* trips, cudaGraphConditionalHandle cond, cudaStream_t s) {
+  k_loop_start<<<1, 32, 0, s>>>(trips, cond);
+  return cudaGetLastError();
+}
+
+cudaError_t loop_next(const KrylovScalars* ks, int* trips, cudaGraphConditionalHandle cond,
+                      int iters_per_trip, cudaStream_t s) {
+  k_loop_next<<<1, 32, 0, s>>>(ks, trips, cond, iters_per_trip);
+  return cudaGetLastError();
+}
+
 cudaError_t pcgc_replace(int n, const double* b, const double* q, const double* m,
                          KrylovVecs& V, KrylovScalars* ks, double* partial, unsigned* counter,
                          cudaStream_t s) {
