@@ -1479,7 +1479,10 @@ int vec_grid(int n) {
 cudaError_t spmv(const PanelView& P, const double* val64, const double* x, double* y,
                  int mode, KrylovScalars* ks, double* partial, unsigned* counter,
                  cudaStream_t s) {
-  const int grid = kRedBlocks;
+  // 32 nodes per CTA (8 warps of 4 sub-warps), at most kRedBlocks CTAs: a
+  // small mesh launches only the CTAs it fills, and its fused dot sums that
+  // many partials
+  const int grid = std::max(1, std::min(kRedBlocks, (P.nact + 31) / 32));
   switch (mode) {
     case 0: k_spmv<double, 0><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
     case 1: k_spmv<double, 1><<<grid, 256, 0, s>>>(P, val64, x, y, ks, partial, counter); break;
