@@ -11,6 +11,7 @@
 // unconverged instances need.
 #include <cuda_runtime.h>
 
+#include "../../include/poromec_gb300.h"
 #include "pm_krylov.h"
 #include "pm_reduce.h"
 
@@ -65,17 +66,24 @@ __device__ __forceinline__ void pair_store(double v, float2* pr, int i) {
 // x = 0, r = b, z = m r, p = z, d = (r, z); conv = tol sqrt|d| (pcg's test)
 // or conv_abs[inst] (a refinement sweep aims at the first sweep's target).
 // Instances outside the sweep are marked done by their first block.
+// With sweep (the device-driven step): b and pcg's test on sweep 0, b_refine
+// and conv_abs on the later sweeps.
 __global__ void __launch_bounds__(256)
     k_bpcg_init(BatchView B, const double* __restrict__ b, const double* __restrict__ m,
                 double* __restrict__ r, double* __restrict__ z, double* __restrict__ p,
                 double* __restrict__ x, float2* __restrict__ pair, double tol,
                 const double* __restrict__ conv_abs, const int* __restrict__ insweep,
-                int maxit) {
+                int maxit, const double* __restrict__ b_refine, const int* __restrict__ sweep) {
   int e0, e1;
   const int inst = seg_range(B, e0, e1);
   if (insweep && !insweep[inst]) {
     if ((int)blockIdx.x == B.blk_ptr[inst] && threadIdx.x == 0) B.done[inst] = 1;
     return;
+  }
+  if (sweep) {
+    const bool refine = *sweep > 0;
+    if (refine) b = b_refine;
+    else conv_abs = nullptr;
   }
   double acc = 0.0;
   for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
@@ -218,13 +226,245 @@ __global__ void __launch_bounds__(256)
   for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) y[i] += x[i];
 }
 
+// ---- control kernels of the device-driven batch step ------------------------
+// One block of kCtlThreads threads each, between the conditional nodes of the
+// step's graph: they keep the host loop's per-instance bookkeeping in device
+// memory and set the loop conditions.  Instance loops are strided, sums and
+// minima are block reductions, so the decisions are the host loop's.
+constexpr int kCtlThreads = 256;
+
+__device__ int ctl_sum(int v, int* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int t = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh[w];
+  return t;
+}
+
+__device__ int ctl_min(int v, int* sh) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int t = v;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = min(t, sh[w]);
+  return t;
+}
+
+__device__ double ctl_max(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = v;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t = fmax(t, sh[w]);
+  return t;
+}
+
+__global__ void __launch_bounds__(kCtlThreads) k_bs_begin(BatchCtl* c, BatchStepArrays A, int ni) {
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    A.active[i] = 1;
+    A.iters[i] = 0;
+    A.nlit[i] = 0;
+  }
+  if (threadIdx.x == 0) *c = BatchCtl{};
+  if (threadIdx.x == 0) c->it = 1;
+}
+
+// cal_residuo_pm (Residuo.f:39-276) per active instance at iteration c->it;
+// the nonlinear loop goes on while an instance is left and no error is set.
+__global__ void __launch_bounds__(kCtlThreads)
+    k_bs_stop(BatchCtl* c, BatchStepArrays A, int ni, int stop_crit, double tol,
+              cudaGraphConditionalHandle cond) {
+  __shared__ int shi[32];
+  __shared__ double shd[32];
+  const int it = c->it;
+  int left = 0;
+  double rmax = 0.0;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    if (!A.active[i]) continue;
+    bool done;
+    if (stop_crit == 1) {
+      const double res = sqrt(A.nr[2 * i] + A.nr[2 * i + 1]);
+      if (it == 1) A.res0[i] = res;
+      else if (it == 2) A.res0[i] = fmax(A.res0[i], res);
+      rmax = fmax(rmax, res);
+      done = A.res0[i] > 0.0 ? res / A.res0[i] < tol : true;
+    } else {
+      const double gresu = sqrt(A.nr[2 * i]), gresp = sqrt(A.nr[2 * i + 1]);
+      if (it == 1) {
+        A.resu0[i] = gresu;
+        A.resp0[i] = gresp;
+      } else if (it == 2) {
+        A.resu0[i] = fmax(A.resu0[i], gresu);
+        A.resp0[i] = fmax(A.resp0[i], gresu);  // as the reference
+      }
+      int istop = 0;
+      if (gresu / A.resu0[i] < tol) istop += 1;
+      if (gresp / A.resp0[i] < tol) istop += 1;
+      done = istop == 2;
+    }
+    if (done) {
+      A.active[i] = 0;
+      A.nlit[i] = it;
+    } else {
+      ++left;
+    }
+  }
+  left = ctl_sum(left, shi);
+  rmax = ctl_max(rmax, shd);
+  if (threadIdx.x == 0) {
+    c->res_max = fmax(c->res_max, rmax);
+    cudaGraphSetConditional(cond, (left > 0 && c->err == 0) ? 1u : 0u);
+  }
+}
+
+// a solve of the active instances: sweep 0, no iterations yet (none after a
+// zero diagonal)
+__global__ void __launch_bounds__(kCtlThreads)
+    k_bs_solve_start(BatchCtl* c, BatchStepArrays A, int ni, cudaGraphConditionalHandle cond) {
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    A.insweep[i] = A.active[i];
+    A.total[i] = 0;
+  }
+  if (threadIdx.x == 0) {
+    c->sweeps = 0;
+    if (c->zdiag && c->err == 0) c->err = PM_E_ZERO_DIAG;
+    cudaGraphSetConditional(cond, c->err == 0 ? 1u : 0u);
+  }
+}
+
+__global__ void k_bs_loop_start(const int* nactive, BatchCtl* c,
+                                cudaGraphConditionalHandle cond) {
+  if (threadIdx.x == 0) {
+    c->trips = 0;
+    cudaGraphSetConditional(cond, *nactive > 0 ? 1u : 0u);
+  }
+}
+
+// after a trip of iters_per_trip iterations: go on while instances are
+// active; every instance stops at maxit, so a trip count past it is an error
+__global__ void k_bs_loop_next(const int* nactive, BatchCtl* c, int maxit, int iters_per_trip,
+                               cudaGraphConditionalHandle cond) {
+  if (threadIdx.x == 0) {
+    const int t = ++c->trips;
+    c->runs_pcg += 1;
+    bool go = *nactive > 0;
+    if (go && (long long)t * iters_per_trip > (long long)maxit + iters_per_trip) {
+      if (c->err == 0) {
+        c->err = PM_E_NOCONV;
+        c->err_inst = -1;
+      }
+      go = false;
+    }
+    cudaGraphSetConditional(cond, go ? 1u : 0u);
+  }
+}
+
+// the end of a sweep: iterations, the first failed instance (in index
+// order), the first sweep's targets; without refinement the solve ends here
+__global__ void __launch_bounds__(kCtlThreads)
+    k_bs_sweep_end(BatchCtl* c, const BatchScalars* __restrict__ bs, BatchStepArrays A, int ni,
+                   int comp, cudaGraphConditionalHandle cond) {
+  __shared__ int shi[32];
+  const int sw = c->sweeps;
+  int bad = ni;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    if (!A.insweep[i]) continue;
+    A.total[i] += bs[i].iter;
+    if (bs[i].conv_flag == 3 || bs[i].conv_flag == 2) bad = min(bad, i);
+    else if (sw == 0) A.conv0[i] = bs[i].conv;
+  }
+  bad = ctl_min(bad, shi);
+  if (threadIdx.x == 0) {
+    c->sweeps = sw + 1;
+    c->runs_sweep += 1;
+    if (bad < ni && c->err == 0) {
+      c->err = PM_E_NOCONV;
+      c->err_inst = bad;
+      c->err_flag = bs[bad].conv_flag;
+      c->err_iters = A.total[bad];
+    }
+    if (c->err != 0 || !comp) cudaGraphSetConditional(cond, 0u);
+  }
+}
+
+// refinement: the instances whose FP64 residual (r, m r) = rn2 is still
+// above the first sweep's target take another sweep, at most max_sweeps
+__global__ void __launch_bounds__(kCtlThreads)
+    k_bs_sweep_next(BatchCtl* c, BatchStepArrays A, int ni, int max_sweeps,
+                    cudaGraphConditionalHandle cond) {
+  __shared__ int shi[32];
+  int again = 0;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    const int in = A.insweep[i] && !(sqrt(fabs(A.rn2[i])) < A.conv0[i]) && A.conv0[i] > 0.0;
+    A.insweep[i] = in;
+    again += in;
+  }
+  again = ctl_sum(again, shi);
+  if (threadIdx.x == 0) {
+    bool go = c->err == 0 && again > 0;
+    if (go && c->sweeps >= max_sweeps) {
+      c->err = PM_E_NOCONV;
+      c->err_inst = -2;
+      go = false;
+    }
+    cudaGraphSetConditional(cond, go ? 1u : 0u);
+  }
+}
+
+// after a solve: per-instance iterations of the step, the solve's largest
+__global__ void __launch_bounds__(kCtlThreads)
+    k_bs_solve_end(BatchCtl* c, BatchStepArrays A, int ni, int comp) {
+  __shared__ int shi[32];
+  int mx = 0;
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+    if (A.active[i]) A.iters[i] += A.total[i];
+    mx = max(mx, A.total[i]);
+  }
+  mx = -ctl_min(-mx, shi);
+  if (threadIdx.x == 0) {
+    c->iters_max = max(c->iters_max, mx);
+    c->refine = comp ? c->sweeps : 0;
+  }
+}
+
+// the nonlinear iteration count: an error past maxnlit
+__global__ void k_bs_nl_next(BatchCtl* c, int maxnlit) {
+  if (threadIdx.x == 0) {
+    c->runs_nl += 1;
+    if (c->err != 0) return;
+    if (c->it >= maxnlit) c->err = PM_E_NLNOCONV;
+    else c->it += 1;
+  }
+}
+
+// the closing passes run when the step met its test without an error
+__global__ void k_bs_finish(BatchCtl* c, const int* elem_err, cudaGraphConditionalHandle cond) {
+  if (threadIdx.x == 0) {
+    c->ok = c->err == 0 && c->zdiag == 0 && *elem_err == 0;
+    cudaGraphSetConditional(cond, c->ok ? 1u : 0u);
+  }
+}
+
 }  // namespace
 
 cudaError_t bpcg_init(const BatchView& B, const double* b, const double* m, KrylovVecs& V,
                       float2* pair, double tol, const double* conv_abs, const int* insweep,
                       int maxit, cudaStream_t s) {
   k_bpcg_init<<<B.nblk, 256, 0, s>>>(B, b, m, V.r, V.z, V.p, V.x, pair, tol, conv_abs, insweep,
-                                      maxit);
+                                      maxit, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t bpcg_init_sweep(const BatchView& B, const double* b, const double* b_refine,
+                            const double* m, KrylovVecs& V, float2* pair, double tol,
+                            const double* conv_abs, const int* insweep, int maxit,
+                            const int* sweep, cudaStream_t s) {
+  k_bpcg_init<<<B.nblk, 256, 0, s>>>(B, b, m, V.r, V.z, V.p, V.x, pair, tol, conv_abs, insweep,
+                                      maxit, b_refine, sweep);
   return cudaGetLastError();
 }
 
@@ -255,6 +495,55 @@ cudaError_t btrue_residual(const BatchView& B, const double* b, const double* q,
 cudaError_t baxpy(const BatchView& B, double* y, const double* x, const int* mask,
                   cudaStream_t s) {
   k_baxpy<<<B.nblk, 256, 0, s>>>(B, y, x, mask);
+  return cudaGetLastError();
+}
+
+cudaError_t bs_begin(BatchCtl* c, const BatchStepArrays& A, int ni, cudaStream_t s) {
+  k_bs_begin<<<1, kCtlThreads, 0, s>>>(c, A, ni);
+  return cudaGetLastError();
+}
+cudaError_t bs_stop(BatchCtl* c, const BatchStepArrays& A, int ni, int stop_crit, double tol,
+                    cudaGraphConditionalHandle cond, cudaStream_t s) {
+  k_bs_stop<<<1, kCtlThreads, 0, s>>>(c, A, ni, stop_crit, tol, cond);
+  return cudaGetLastError();
+}
+cudaError_t bs_solve_start(BatchCtl* c, const BatchStepArrays& A, int ni,
+                           cudaGraphConditionalHandle cond, cudaStream_t s) {
+  k_bs_solve_start<<<1, kCtlThreads, 0, s>>>(c, A, ni, cond);
+  return cudaGetLastError();
+}
+cudaError_t bs_loop_start(const BatchView& B, BatchCtl* c, cudaGraphConditionalHandle cond,
+                          cudaStream_t s) {
+  k_bs_loop_start<<<1, 32, 0, s>>>(B.nactive, c, cond);
+  return cudaGetLastError();
+}
+cudaError_t bs_loop_next(const BatchView& B, BatchCtl* c, int maxit, int iters_per_trip,
+                         cudaGraphConditionalHandle cond, cudaStream_t s) {
+  k_bs_loop_next<<<1, 32, 0, s>>>(B.nactive, c, maxit, iters_per_trip, cond);
+  return cudaGetLastError();
+}
+cudaError_t bs_sweep_end(BatchCtl* c, const BatchView& B, const BatchStepArrays& A, int ni,
+                         bool comp, cudaGraphConditionalHandle cond, cudaStream_t s) {
+  k_bs_sweep_end<<<1, kCtlThreads, 0, s>>>(c, B.bs, A, ni, comp ? 1 : 0, cond);
+  return cudaGetLastError();
+}
+cudaError_t bs_sweep_next(BatchCtl* c, const BatchStepArrays& A, int ni, int max_sweeps,
+                          cudaGraphConditionalHandle cond, cudaStream_t s) {
+  k_bs_sweep_next<<<1, kCtlThreads, 0, s>>>(c, A, ni, max_sweeps, cond);
+  return cudaGetLastError();
+}
+cudaError_t bs_solve_end(BatchCtl* c, const BatchStepArrays& A, int ni, bool comp,
+                         cudaStream_t s) {
+  k_bs_solve_end<<<1, kCtlThreads, 0, s>>>(c, A, ni, comp ? 1 : 0);
+  return cudaGetLastError();
+}
+cudaError_t bs_nl_next(BatchCtl* c, int maxnlit, cudaStream_t s) {
+  k_bs_nl_next<<<1, 32, 0, s>>>(c, maxnlit);
+  return cudaGetLastError();
+}
+cudaError_t bs_finish(BatchCtl* c, const int* elem_err, cudaGraphConditionalHandle cond,
+                      cudaStream_t s) {
+  k_bs_finish<<<1, 32, 0, s>>>(c, elem_err, cond);
   return cudaGetLastError();
 }
 

@@ -64,10 +64,12 @@ __global__ void k_predict(int nnode, const int32_t* __restrict__ fnno, double* _
   }
 }
 
-// delta_update_pm (Predict.f:159-215): du += x on free dofs
+// delta_update_pm (Predict.f:159-215): du += x on free dofs (nothing when
+// *skip is set: a device-driven step whose solve failed)
 __global__ void k_delta_update(int nnode, const int32_t* __restrict__ eq,
                                const int32_t* __restrict__ fnno, double* __restrict__ u,
-                               const double* __restrict__ x) {
+                               const double* __restrict__ x, const int* skip = nullptr) {
+  if (skip && *skip) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nnode; i += gridDim.x * blockDim.x) {
     const int nj = fnno[i] == 1 ? 4 : 3;
     for (int j = 0; j < nj; ++j) {
@@ -1129,6 +1131,19 @@ int batch_setup(Handle* h) {
   PM_TRY(up(&h->d_insweep, (int*)nullptr, (size_t)ni));
   PM_TRY(up(&h->d_conv0, (double*)nullptr, (size_t)ni));
   PM_TRY(up(&h->d_bnorms, (double*)nullptr, (size_t)2 * ni));
+  pm::BatchStepArrays& A = h->bsa;
+  PM_TRY(up(&h->d_bctl, (pm::BatchCtl*)nullptr, 1));
+  PM_TRY(up(&A.active, (int*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.total, (int*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.iters, (int*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.nlit, (int*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.res0, (double*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.resu0, (double*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.resp0, (double*)nullptr, (size_t)ni));
+  PM_TRY(up(&A.nr, (double*)nullptr, (size_t)2 * ni));
+  PM_TRY(up(&A.rn2, (double*)nullptr, (size_t)ni));
+  A.insweep = h->d_insweep;
+  A.conv0 = h->d_conv0;
   h->b_iters.assign(ni, 0);
   h->b_nlit.assign(ni, 0);
   return PM_OK;
@@ -1139,6 +1154,8 @@ int batch_setup(Handle* h) {
 // operator inside the FP64 refinement of krylov(), per instance: after the
 // sweep, r = b - A64 x in FP64, and the instances whose sqrt|(r, m r)| is
 // still above their first sweep's target solve A dx = r to that target.
+constexpr int kMaxBatchSweeps = 8;  // refinement sweeps of a batch solve
+
 int krylov_batch(Handle* h, const double* d_b, double* d_x, double tol, int maxit, bool comp,
                  const std::vector<int>& active, pm_step_info* info) {
   const int n = h->neq, ni = h->ninst;
@@ -1162,7 +1179,6 @@ int krylov_batch(Handle* h, const double* d_b, double* d_x, double tol, int maxi
   std::vector<double> conv0(ni, 0.0), rn2(ni, 0.0);
   std::vector<pm::BatchScalars> bs(ni);
   std::vector<int> total(ni, 0);
-  const int kMaxSweeps = 8;
   int sweeps = 0;
   for (;;) {
     PM_CUDA(cudaMemcpyAsync(h->d_insweep, insweep.data(), sizeof(int) * ni,
@@ -1218,7 +1234,7 @@ int krylov_batch(Handle* h, const double* d_b, double* d_x, double tol, int maxi
     if (h->debug)
       fprintf(stderr, "batch refine sweep %d: %d instances above target\n", sweeps, again);
     if (again == 0) break;
-    if (sweeps >= kMaxSweeps) {
+    if (sweeps >= kMaxBatchSweeps) {
       h->err = "batch refinement: FP64 residual above target after " +
                std::to_string(sweeps) + " sweeps";
       return PM_E_NOCONV;
@@ -1370,6 +1386,12 @@ void free_all(Handle* h) {
                   (void*)h->d_conv0, (void*)h->d_bnorms})
     if (p) cudaFree(p);
   if (h->minresc_graph) cudaGraphExecDestroy(h->minresc_graph);
+  if (h->bstep_exec) cudaGraphExecDestroy(h->bstep_exec);
+  const pm::BatchStepArrays& A = h->bsa;
+  for (void* p : {(void*)h->d_bctl, (void*)A.active, (void*)A.total, (void*)A.iters,
+                  (void*)A.nlit, (void*)A.res0, (void*)A.resu0, (void*)A.resp0, (void*)A.nr,
+                  (void*)A.rn2})
+    if (p) cudaFree(p);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1432,11 +1454,294 @@ int porosity_pass(Handle* h, cudaStream_t s) {
   return PM_OK;
 }
 
+// ---- a batch time step as one CUDA graph ---------------------------------------
+// Launches captured from the handle's stream into graph g after node dep,
+// and conditional nodes added between the captures.
+struct GraphCap {
+  cudaStream_t s;
+  cudaGraph_t g;
+  bool ok;
+  cudaGraphNode_t dep = nullptr;  // the node the next capture or node follows
+
+  template <typename Fn>
+  void seg(Fn fn) {
+    if (!ok) return;
+    ok = cudaStreamBeginCaptureToGraph(s, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0,
+                                       cudaStreamCaptureModeRelaxed) == cudaSuccess;
+    if (!ok) return;
+    const int rc = fn();
+    cudaStreamCaptureStatus st{};
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    const bool info =
+        cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &deps, nullptr, &nd) == cudaSuccess;
+    const cudaGraphNode_t leaf = (info && nd == 1) ? deps[0] : nullptr;
+    cudaGraph_t out = nullptr;
+    const bool ended = cudaStreamEndCapture(s, &out) == cudaSuccess;
+    ok = rc == PM_OK && leaf != nullptr && ended;
+    if (ok) dep = leaf;
+  }
+  // a conditional node after dep; returns its body graph
+  cudaGraph_t cond(cudaGraphConditionalHandle c, cudaGraphConditionalNodeType type) {
+    if (!ok) return nullptr;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = c;
+    np.conditional.type = type;
+    np.conditional.size = 1;
+    cudaGraphNode_t node{};
+    ok = cudaGraphAddNode(&node, g, dep ? &dep : nullptr, nullptr, dep ? 1 : 0, &np) ==
+         cudaSuccess;
+    if (!ok) return nullptr;
+    dep = node;
+    return np.conditional.phGraph_out[0];
+  }
+  cudaGraphConditionalHandle handle() {
+    cudaGraphConditionalHandle c{};
+    if (ok) ok = cudaGraphConditionalHandleCreate(&c, g, 0, 0) == cudaSuccess;
+    return c;
+  }
+};
+
+int kernel_nodes(cudaGraph_t g) {
+  if (!g) return 0;
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return 0;
+  std::vector<cudaGraphNode_t> v(n);
+  if (n && cudaGraphGetNodes(g, v.data(), &n) != cudaSuccess) return 0;
+  int k = 0;
+  for (cudaGraphNode_t x : v) {
+    cudaGraphNodeType t{};
+    if (cudaGraphNodeGetType(x, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+// The batch step of step_batch as one CUDA graph, captured every step (the
+// step's t, dt and settings are kernel arguments) and launched once:
+//   load, isw 4 and predictor passes; b = b0 - K u (assembly or residual);
+//   per-instance stop test;
+//   WHILE an instance is left: preconditioner;
+//     WHILE a refinement sweep is wanted: bpcg_init;
+//       WHILE an instance is iterating: kGraphIters PCG iterations;
+//       sweep bookkeeping, x += dx, [compensated: FP64 residual, next sweep];
+//     du += x; b = b0 - K u; stop test;
+//   IF no error: porosity and state updates.
+// The loop conditions are set by the control kernels of pm_batch.cu from
+// device-side state (BatchCtl, BatchStepArrays) that the host reads once,
+// after the graph.  *ran is false when the graph was not built (the step's
+// settings need the host loop, or the driver refused a part): step_batch's
+// host loop then runs the step.
+int step_batch_graph(Handle* h, int maxnlit, double tol, int stop_crit, int precond,
+                     double solvtol, int maxit, int reassemble, pm_step_info* info, bool* ran) {
+  *ran = false;
+  const bool comp = h->precision == PM_FP32C_REFINE;
+  if (h->bstep_failed || std::getenv("PM_BATCH_HOST_STEP") || !h->d_bctl ||
+      (stop_crit != 1 && stop_crit != 2) || (precond != 2 && precond != 5) ||
+      (comp && (!h->P.valh || h->shape == 0)))
+    return PM_OK;
+  cudaStream_t s = h->stream;
+  pm::Dev& D = h->D;
+  const int ni = h->ninst, n = h->neq;
+  // host bookkeeping that the capture advances; put back if the graph is not run
+  const int istep0 = h->istep;
+  const double t0 = h->t, adt0 = h->assembled_dt;
+  const bool asm0 = h->assembled, asm32 = h->assembled32, asmC = h->assembledC;
+  const int64_t launches0 = h->launches;
+  h->istep += 1;
+  h->t = h->t + h->dt;
+  const bool need_K = reassemble || !h->assembled || h->assembled_dt != h->dt;
+  const bool split = comp && (need_K || !h->assembledC);
+  pm::BatchCtl* c = h->d_bctl;
+  const pm::BatchStepArrays A = h->bsa;
+  const pm::BatchView& B = h->B;
+  pm::KrylovVecs& V = D.kv;
+  float2* pair = D.kv32.c;
+  const pm::PanelView PB = h->P.bview(), P = h->P.view();
+  const pm::CompVals C = h->P.comp(h->shape);
+  const int nb = grid_for(h->nnode);
+
+  cudaGraph_t g = nullptr;
+  GraphCap top{s, nullptr, cudaGraphCreate(&g, 0) == cudaSuccess};
+  top.g = g;
+  const cudaGraphConditionalHandle c_nl = top.handle(), c_ok = top.handle();
+  top.seg([&]() -> int {
+    PM_CUDA(pm::bs_begin(c, A, ni, s));
+    k_pload<<<nb, 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.nload, D.f, D.u, D.b0, D.load,
+                               D.fload, h->maxt, D.x, h->t, h->dt, h->gravity_mod);
+    PM_CUDA(cudaGetLastError());
+    PM_TRY(rhs4(h, D.u, D.b0));
+    if (h->fstress0) PM_CUDA(pm::axpy_into(n, D.b0, D.bst0, 1.0, s));
+    k_predict<<<nb, 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(cudaMemcpyAsync(D.b, D.b0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    if (need_K) PM_TRY(assemble_K(h, D.u, D.b));  // b -= K u in the same launch
+    else PM_TRY(residual(h, D.u, D.b));
+    if (split) PM_CUDA(pm::split_values(h->P.nnz, h->P.val, h->P.valh, h->P.vall, s));
+    PM_CUDA(pm::bresnorms(B, D.b, D.dofkind, A.nr, s));
+    PM_CUDA(pm::bs_stop(c, A, ni, stop_crit, tol, c_nl, s));
+    return PM_OK;
+  });
+  const cudaGraph_t g_nl = top.cond(c_nl, cudaGraphCondTypeWhile);
+  GraphCap nl{s, g_nl, top.ok};
+  const cudaGraphConditionalHandle c_sw = nl.handle();
+  nl.seg([&]() -> int {
+    PM_CUDA(pm::panel_diag(P, h->P.val, nullptr, D.ad, s));
+    PM_CUDA(pm::precond(n, D.ad, D.m, precond == 5, &c->zdiag, s));
+    PM_CUDA(cudaMemsetAsync(D.xs, 0, sizeof(double) * n, s));
+    PM_CUDA(pm::bs_solve_start(c, A, ni, c_sw, s));
+    return PM_OK;
+  });
+  const cudaGraph_t g_sw = nl.cond(c_sw, cudaGraphCondTypeWhile);
+  GraphCap sw{s, g_sw, nl.ok};
+  const cudaGraphConditionalHandle c_pcg = sw.handle();
+  sw.seg([&]() -> int {
+    PM_CUDA(cudaMemsetAsync(B.nactive, 0, sizeof(int), s));
+    PM_CUDA(pm::bpcg_init_sweep(B, D.b, D.rr, D.m, V, comp ? pair : nullptr, solvtol, A.conv0,
+                                A.insweep, maxit, &c->sweeps, s));
+    PM_CUDA(pm::bs_loop_start(B, c, c_pcg, s));
+    return PM_OK;
+  });
+  const cudaGraph_t g_pcg = sw.cond(c_pcg, cudaGraphCondTypeWhile);
+  GraphCap pcg{s, g_pcg, sw.ok};
+  pcg.seg([&]() -> int {
+    for (int k = 0; k < kGraphIters; ++k)
+      PM_CUDA(pm::bpcg_iteration(PB, h->P.val, comp ? &C : nullptr, B, D.m, V, pair, s));
+    PM_CUDA(pm::bs_loop_next(B, c, maxit, kGraphIters, c_pcg, s));
+    return PM_OK;
+  });
+  sw.ok = sw.ok && pcg.ok;
+  sw.seg([&]() -> int {
+    PM_CUDA(pm::bs_sweep_end(c, B, A, ni, comp, c_sw, s));
+    PM_CUDA(pm::baxpy(B, D.xs, V.x, A.insweep, s));
+    if (comp) {
+      PM_CUDA(pm::spmv(P, h->P.val, D.xs, D.dx, 0, nullptr, nullptr, nullptr, s));
+      PM_CUDA(pm::btrue_residual(B, D.b, D.dx, D.m, D.rr, A.rn2, s));
+      PM_CUDA(pm::bs_sweep_next(c, A, ni, kMaxBatchSweeps, c_sw, s));
+    }
+    return PM_OK;
+  });
+  nl.ok = nl.ok && sw.ok;
+  nl.seg([&]() -> int {
+    PM_CUDA(pm::bs_solve_end(c, A, ni, comp, s));
+    k_delta_update<<<nb, 256, 0, s>>>(h->nnode, D.eq, D.fnno, D.u, D.xs, &c->err);
+    PM_CUDA(cudaGetLastError());
+    PM_CUDA(pm::bs_nl_next(c, maxnlit, s));
+    PM_CUDA(cudaMemcpyAsync(D.b, D.b0, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    PM_TRY(residual(h, D.u, D.b));
+    PM_CUDA(pm::bresnorms(B, D.b, D.dofkind, A.nr, s));
+    PM_CUDA(pm::bs_stop(c, A, ni, stop_crit, tol, c_nl, s));
+    return PM_OK;
+  });
+  top.ok = top.ok && nl.ok;
+  top.seg([&]() -> int {
+    PM_CUDA(pm::bs_finish(c, D.err, c_ok, s));
+    return PM_OK;
+  });
+  const cudaGraph_t g_ok = top.cond(c_ok, cudaGraphCondTypeIf);
+  GraphCap fin{s, g_ok, top.ok};
+  fin.seg([&]() -> int {
+    PM_TRY(porosity_pass(h, s));
+    k_update_res<<<nb, 256, 0, s>>>(h->nnode, D.fnno, D.u, D.u0, D.dp);
+    PM_CUDA(cudaGetLastError());
+    return PM_OK;
+  });
+  bool ok = top.ok && fin.ok;
+  const int kn_top = ok ? kernel_nodes(g) : 0, kn_nl = ok ? kernel_nodes(g_nl) : 0;
+  const int kn_sw = ok ? kernel_nodes(g_sw) : 0, kn_pcg = ok ? kernel_nodes(g_pcg) : 0;
+  const int kn_ok = ok ? kernel_nodes(g_ok) : 0;
+  if (ok) {
+    if (h->bstep_exec) cudaGraphExecDestroy(h->bstep_exec);
+    h->bstep_exec = nullptr;
+    ok = cudaGraphInstantiate(&h->bstep_exec, g, 0) == cudaSuccess;
+  }
+  if (g) cudaGraphDestroy(g);
+  h->launches = launches0;
+  if (!ok) {
+    cudaGetLastError();  // the refusal is not this step's error
+    h->bstep_failed = true;
+    h->istep = istep0;
+    h->t = t0;
+    h->assembled = asm0;
+    h->assembled32 = asm32;
+    h->assembledC = asmC;
+    h->assembled_dt = adt0;
+    if (h->debug) fprintf(stderr, "batch step graph unavailable: host loop\n");
+    return PM_OK;
+  }
+  *ran = true;
+  if (split) h->assembledC = true;
+  PM_CUDA(cudaEventRecord(h->ev[0], s));
+  PM_CUDA(cudaGraphLaunch(h->bstep_exec, s));
+  PM_CUDA(cudaEventRecord(h->ev[1], s));
+  pm::BatchCtl ctl{};
+  int elem_err = 0;
+  std::vector<int> iters(ni), nlit(ni);
+  PM_CUDA(cudaMemcpyAsync(&ctl, c, sizeof(ctl), cudaMemcpyDeviceToHost, s));
+  PM_CUDA(cudaMemcpyAsync(&elem_err, D.err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  PM_CUDA(cudaMemcpyAsync(iters.data(), A.iters, sizeof(int) * ni, cudaMemcpyDeviceToHost, s));
+  PM_CUDA(cudaMemcpyAsync(nlit.data(), A.nlit, sizeof(int) * ni, cudaMemcpyDeviceToHost, s));
+  PM_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+  h->launches += kn_top + (int64_t)kn_nl * ctl.runs_nl + (int64_t)kn_sw * ctl.runs_sweep +
+                 (int64_t)kn_pcg * ctl.runs_pcg + (ctl.ok ? kn_ok : 0);
+  h->timers[0] = h->timers[1] = h->timers[2] = 0.0;
+  h->timers[3] = ms;
+  h->timers[7] = (double)(h->launches - launches0);
+  if (elem_err) {
+    PM_CUDA(cudaMemsetAsync(D.err, 0, sizeof(int), s));
+    h->err = "element Jacobian determinant <= 1e-14";
+    return PM_E_DET;
+  }
+  if (ctl.err == PM_E_ZERO_DIAG) {
+    h->err = "zero diagonal coefficient";
+    return PM_E_ZERO_DIAG;
+  }
+  if (ctl.err == PM_E_NOCONV) {
+    if (ctl.err_inst >= 0) {
+      h->err = "batch PCG, instance " + std::to_string(ctl.err_inst) +
+               (ctl.err_flag == 3 ? ": breakdown (non-finite recurrence)"
+                                  : ": no convergence reached after " +
+                                        std::to_string(ctl.err_iters) + " iterations");
+      if (info) info->iters = ctl.err_iters;
+    } else if (ctl.err_inst == -1) {
+      h->err = "batch PCG: iteration count past maxit with instances still active";
+    } else {
+      h->err = "batch refinement: FP64 residual above target after " +
+               std::to_string(kMaxBatchSweeps) + " sweeps";
+    }
+    return PM_E_NOCONV;
+  }
+  if (ctl.err == PM_E_NLNOCONV) {
+    h->err = "nonlinear iteration: no convergence after " + std::to_string(ctl.it) +
+             " iterations (batch)";
+    return PM_E_NLNOCONV;
+  }
+  h->b_iters = iters;
+  h->b_nlit = nlit;
+  if (info) {
+    pm_step_info loc{};
+    loc.res_u = ctl.res_max;
+    loc.iters = ctl.iters_max;
+    loc.refine = ctl.refine;
+    loc.nlit = ctl.it;
+    *info = loc;
+  }
+  return PM_OK;
+}
+
 int step_batch(Handle* h, int maxnlit, double tol, int stop_crit, int solver, int precond,
                double solvtol, int maxit, int reassemble, pm_step_info* info) {
   if (solver != 1 || h->precision == PM_FP32_REFINE) {
     h->err = "a batch of meshes is solved by PCG (solver 1) in PM_FP64 or PM_FP32C_REFINE";
     return PM_E_ARG;
+  }
+  {
+    bool ran = false;
+    const int rc = step_batch_graph(h, maxnlit, tol, stop_crit, precond, solvtol, maxit,
+                                    reassemble, info, &ran);
+    if (ran || rc != PM_OK) return rc;
   }
   cudaStream_t s = h->stream;
   pm::Dev& D = h->D;

@@ -220,6 +220,12 @@ struct Handle {
   // driver cannot build it)
   cudaGraphExec_t pcg_loop = nullptr;
   bool pcg_loop_failed = false;
+  // a batch time step as one graph (step_batch_graph): control state and
+  // per-instance arrays on the device, the executable graph of the last step
+  pm::BatchCtl* d_bctl = nullptr;
+  pm::BatchStepArrays bsa{};
+  cudaGraphExec_t bstep_exec = nullptr;
+  bool bstep_failed = false;
   double timers[8] = {0};
   int64_t launches = 0;        // kernels launched by the library (all calls)
   std::string err;

@@ -263,11 +263,60 @@ cudaError_t bpcg_init(const BatchView& B, const double* b, const double* m, Kryl
 cudaError_t bpcg_iteration(const PanelView& P, const double* val64, const CompVals* C,
                            const BatchView& B, const double* m, KrylovVecs& V, float2* pair,
                            cudaStream_t s);
+// bpcg_init for a refinement sweep decided on the device: b and pcg's test
+// when *sweep = 0, b_refine and conv_abs after
+cudaError_t bpcg_init_sweep(const BatchView& B, const double* b, const double* b_refine,
+                            const double* m, KrylovVecs& V, float2* pair, double tol,
+                            const double* conv_abs, const int* insweep, int maxit,
+                            const int* sweep, cudaStream_t s);
 cudaError_t bresnorms(const BatchView& B, const double* b, const int32_t* kind, double* out,
                       cudaStream_t s);
 cudaError_t btrue_residual(const BatchView& B, const double* b, const double* q,
                            const double* m, double* r, double* out, cudaStream_t s);
 cudaError_t baxpy(const BatchView& B, double* y, const double* x, const int* mask,
                   cudaStream_t s);
+
+// ---- a batch time step driven on the device (one CUDA graph per step) ----
+// Control state, set by the control kernels between the graph's
+// conditional nodes and read by the host once the step's graph has run.
+struct BatchCtl {
+  int it;          // nonlinear iteration (1-based)
+  int sweeps;      // refinement sweeps of the current solve
+  int trips;       // PCG loop trips of the current sweep
+  int err;         // 0 or the step's status (PM_E_NOCONV, PM_E_NLNOCONV, PM_E_ZERO_DIAG)
+  int err_inst;    // Krylov failure: its instance (-1 the trip bound, -2 the sweeps)
+  int err_flag;    //   and the instance's conv_flag
+  int err_iters;   //   and its iterations
+  int zdiag;       // zero diagonal seen by the preconditioner
+  int refine;      // sweeps of the last solve (compensated operator)
+  int iters_max;   // the largest per-instance iteration count of a solve
+  int runs_nl, runs_sweep, runs_pcg, ok;  // trips of each loop, closing passes run
+  double res_max;  // the largest residual norm of the stop test (stop_crit 1)
+};
+
+// per-instance device arrays of the step (ni each; nr 2 ni)
+struct BatchStepArrays {
+  int *active, *insweep, *total, *iters, *nlit;
+  double *conv0, *res0, *resu0, *resp0, *nr, *rn2;
+};
+
+cudaError_t bs_begin(BatchCtl* c, const BatchStepArrays& A, int ni, cudaStream_t s);
+cudaError_t bs_stop(BatchCtl* c, const BatchStepArrays& A, int ni, int stop_crit, double tol,
+                    cudaGraphConditionalHandle cond, cudaStream_t s);
+cudaError_t bs_solve_start(BatchCtl* c, const BatchStepArrays& A, int ni,
+                           cudaGraphConditionalHandle cond, cudaStream_t s);
+cudaError_t bs_loop_start(const BatchView& B, BatchCtl* c, cudaGraphConditionalHandle cond,
+                          cudaStream_t s);
+cudaError_t bs_loop_next(const BatchView& B, BatchCtl* c, int maxit, int iters_per_trip,
+                         cudaGraphConditionalHandle cond, cudaStream_t s);
+cudaError_t bs_sweep_end(BatchCtl* c, const BatchView& B, const BatchStepArrays& A, int ni,
+                         bool comp, cudaGraphConditionalHandle cond, cudaStream_t s);
+cudaError_t bs_sweep_next(BatchCtl* c, const BatchStepArrays& A, int ni, int max_sweeps,
+                          cudaGraphConditionalHandle cond, cudaStream_t s);
+cudaError_t bs_solve_end(BatchCtl* c, const BatchStepArrays& A, int ni, bool comp,
+                         cudaStream_t s);
+cudaError_t bs_nl_next(BatchCtl* c, int maxnlit, cudaStream_t s);
+cudaError_t bs_finish(BatchCtl* c, const int* elem_err, cudaGraphConditionalHandle cond,
+                      cudaStream_t s);
 
 }  // namespace pm

@@ -125,6 +125,80 @@ def test_batch_steps_match_oracle(precision, bar):
             assert np.abs(part[:, sl] - ref).max() <= bar * np.abs(ref).max(), (k, sl)
 
 
+def _steps(pb, precision, host_loop, steps, **kw):
+    """A batch stepped `steps` times by the device-driven step graph or by the
+    host loop (PM_BATCH_HOST_STEP); returns the state, per-instance counts,
+    step infos (or the PMError of a failed step) and timers."""
+    old = os.environ.pop("PM_BATCH_HOST_STEP", None)
+    try:
+        if host_loop:
+            os.environ["PM_BATCH_HOST_STEP"] = "1"
+        m = pg.from_problem(pb)
+        m.set_precision(precision)
+        out = []
+        for _ in range(steps):
+            try:
+                i = m.step(**kw)
+                out.append((i.nlit, i.iters, i.refine, m.batch_iters(), m.timers()))
+            except pg.PMError as e:
+                out.append((e.status, str(e)))
+                break
+        u = m.get_state()
+        m.close()
+        return u, out
+    finally:
+        os.environ.pop("PM_BATCH_HOST_STEP", None)
+        if old is not None:
+            os.environ["PM_BATCH_HOST_STEP"] = old
+
+
+@pytest.mark.parametrize("precision", [pg.capi.PM_FP64, pg.capi.PM_FP32C_REFINE])
+def test_batch_step_graph_matches_host_loop(instances, precision, monkeypatch):
+    """The batch step as one CUDA graph (conditional nodes for the nonlinear
+    loop, the refinement sweeps and the PCG iterations, decided on the
+    device) runs the host loop's kernels in the host loop's order: the same
+    state bit for bit, the same per-instance iterations and nonlinear
+    counts.  The compensated SpMV shape is fixed so both handles run the same
+    kernel (the autotuner times kernels)."""
+    monkeypatch.setenv("PM_SPMV_SHAPE", "314")
+    pb = meshgen.union_problem(instances)
+    kw = dict(maxnlit=500, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=1e-11,
+              maxit=100000)
+    ug, og = _steps(pb, precision, False, 4, **kw)
+    uh, oh = _steps(pb, precision, True, 4, **kw)
+    for a, b in zip(ug, uh):
+        assert np.array_equal(a, b)
+    graph_steps = 0
+    for (gl, gi, gr, (git, gnl), gt), (hl, hi, hr, (hit, hnl), ht) in zip(og, oh):
+        assert (gl, gi, gr) == (hl, hi, hr)
+        assert np.array_equal(git, hit) and np.array_equal(gnl, hnl)
+        assert ht[0] > 0.0  # the host loop times its phases
+        graph_steps += gt[0] == 0.0 and gt[3] > 0.0  # the graph: one time for the step
+    # the compensated handle's first step tunes and splits on the host loop
+    assert graph_steps >= 3
+
+
+@pytest.mark.parametrize("case", ["maxnlit", "maxit"])
+def test_batch_step_graph_errors_match_host_loop(instances, case):
+    """Failures decided on the device give the host loop's status, message
+    and state: the nonlinear limit (maxnlit 1 with an unreachable test) and
+    the PCG iteration limit (maxit 3)."""
+    pb = meshgen.union_problem(instances)
+    kw = dict(maxnlit=500, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=1e-11,
+              maxit=100000)
+    if case == "maxnlit":
+        kw.update(maxnlit=1, tol=1e-30)
+        status = 5
+    else:
+        kw.update(maxit=3)
+        status = 4
+    ug, og = _steps(pb, pg.capi.PM_FP64, False, 2, **kw)
+    uh, oh = _steps(pb, pg.capi.PM_FP64, True, 2, **kw)
+    assert og[-1] == oh[-1] and og[-1][0] == status
+    for a, b in zip(ug, uh):
+        assert np.array_equal(a, b)
+
+
 def test_batch_rejects_minres(instances):
     mb = pg.from_problem(meshgen.union_problem(instances))
     mb.pform(2, True, False, np.zeros((mb.nnode, 4)), None)
