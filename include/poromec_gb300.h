@@ -96,7 +96,12 @@ int pm_reord(int nnode, int numel, int nen, const int32_t* ix, int32_t* num);
  * inst_node_ptr[ninst] = nnode) and each element lies inside one instance.
  * pm_solve and pm_step then solve every instance independently, as if each
  * were its own handle (own PCG scalars, stopping test, nonlinear test), in
- * shared launches: PCG (solver 1) only, in PM_FP64 or PM_FP32C_REFINE. */
+ * shared launches: PCG (solver 1) only, in PM_FP64 or PM_FP32C_REFINE.
+ * pm_step on a batch captures the whole time step into one CUDA graph whose
+ * loops (nonlinear iterations, refinement sweeps, PCG iterations) are decided
+ * on the device, and launches it once; with PM_BATCH_HOST_STEP set in the
+ * environment, on stop_crit other than 1 or 2, and on the first compensated
+ * step (SpMV shape tuning) the host drives the same kernels instead. */
 int pm_batch_create(int nnode, int nnodev, int numel, int nen, int nenv, int ndm, int ndf,
                     const int32_t* ix, const int32_t* id, const int32_t* fnno,
                     const double* x, int numat, const int32_t* ie, const double* e,
@@ -272,7 +277,8 @@ int pm_adjoint_grad_dev(pm_handle h, const double* d_lam, const double* d_un,
 
 /* Timing of the last pm_step phases in milliseconds (CUDA events):
  * [0] pload+isw4, [1] assembly (isw2 lhs), [2] isw2 residual passes,
- * [3] solve, [4] Krylov iterations of all the solves of the last single-mesh
+ * [3] solve (a batch step run as one graph: the whole step, [0]-[2] are 0),
+ * [4] Krylov iterations of all the solves of the last single-mesh
  * pm_step (the step's info->iters counts its last solve only; 0 for a batch),
  * [5] device time of the last Krylov solve,
  * [6] Krylov iterations of the last solve, [7] kernels launched by the step. */
