@@ -89,13 +89,17 @@ def parse(argv=None):
                     choices=["cube", "batched", "adjoint", "tetra"],
                     help="batched: only the batch of independent cubes; adjoint: the "
                          "gradient of a 50-step misfit on a 40^3 cube and its finite-"
-                         "difference check; tetra: rpsqmr steps on the unstructured "
-                         "tetra10 box, FP64 and compensated (each its own line)")
+                         "difference check; tetra: steps on the unstructured tetra10 box, "
+                         "FP64 and compensated (its own line)")
     ap.add_argument("--tetra-mixed", action="store_true",
-                    help="also time the tetra box with the compensated operator: rpsqmr's "
-                         "refinement restarts cost far more iterations than they save there")
+                    help="with --tetra-solver 11, also time rpsqmr on the compensated "
+                         "operator: its refinement restarts cost far more iterations than "
+                         "they save there")
     ap.add_argument("--tetra-n", type=int, default=48,
                     help="hex cells per edge of the tetra workload (6 tets each)")
+    ap.add_argument("--tetra-solver", type=int, default=1, choices=[1, 11],
+                    help="Krylov solver of the tetra workload: 1 pcg (with the compensated "
+                         "operator and FP64 rpsqmr beside it), 11 rpsqmr")
     ap.add_argument("--fd-dirs", type=int, default=2,
                     help="finite-difference directions of the adjoint workload")
     ap.add_argument("--adj-n", type=int, default=40)
@@ -587,23 +591,28 @@ def run_adjoint(args):
 def tetra_leg(args, steps, warmup):
     """Unstructured tetra10 workload: --tetra-n^3 hex cells on a 2 x 2 x 1 m box
     split in 6 Kuhn tets, interior vertices jittered, two layers, a point
-    source, dt 60 s.  Solver: rpsqmr (solver 11, the reference's default) with
-    the diagonal preconditioner, at the cube's PCG tolerance and nonlinear
-    settings; diagonally preconditioned MINRES
-    needs 2e4 iterations per step at 4^3 and 4e5 at 8^3 on this problem and
-    PCG fails the nonlinear test at 8^3 (the oracle shows the same), so
-    rpsqmr stands in for them.  FP64 steps after warm-up, timed on the device
-    with inputs resident; with --tetra-mixed the same steps from the same
-    state with the compensated operator in FP64 refinement (PM_FP32C_REFINE):
-    rpsqmr's refinement restarts its Krylov space, which at this tolerance
-    costs more iterations than the cheaper product saves."""
+    source, dt 60 s, at the cube's PCG tolerance and nonlinear settings.
+    Solver (--tetra-solver): pcg (solver 1, default) with the diagonal
+    preconditioner, or rpsqmr (solver 11, the reference's default solver).
+    Diagonally preconditioned MINRES as the reference implements it (the
+    Lanczos alpha taken in absolute value) needs 2e4 iterations per step at
+    4^3 and 4e5 at 8^3 on this indefinite system (the oracle shows the same),
+    so pcg stands in for it; on this machine pcg takes ~25 % fewer iterations
+    than rpsqmr and reaches the same state (the oracle shows that too).  FP64
+    steps after warm-up, timed on the device with inputs resident; then the
+    same steps from the same state with the compensated operator in FP64
+    refinement (PM_FP32C_REFINE: pcg with residual replacement; for rpsqmr
+    only with --tetra-mixed, whose refinement restarts its Krylov space and
+    at this tolerance costs more iterations than the cheaper product saves);
+    with pcg, also FP64 rpsqmr from the same state for comparison."""
     import torch
     import poromec_gb300 as pg
     from poromec_gb300 import meshgen
     pb = meshgen.tetra_problem(args.tetra_n)
     m = pg.from_problem(pb)
     dt = float(pb["dt"])
-    kw = step_kwargs(args, solver=11)
+    kw = step_kwargs(args, solver=args.tetra_solver)
+    sname = {1: "pcg", 11: "rpsqmr"}[args.tetra_solver]
     log("tetra set up: %d equations" % m.neq)
     for _ in range(warmup):
         m.step(**kw)
@@ -614,28 +623,33 @@ def tetra_leg(args, steps, warmup):
         m.set_state(*snap)
         m.set_env(pb["gravity"], dt, warmup * dt, warmup)
 
-    def timed():
+    def timed(skw, what):
         its = []
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(steps):
-            m.step(**kw)
+            m.step(**skw)
             its.append(int(m.timers()[4]))
-            log("tetra step: %d iterations" % its[-1])
+            log("tetra %s step: %d iterations" % (what, its[-1]))
         torch.cuda.synchronize()
         return time.perf_counter() - t0, its
 
-    mixed = None
+    mixed = qmr = None
     with ClockSampler(0) as clk:
         restore()
-        t64, its64 = timed()
+        t64, its64 = timed(kw, sname)
         u64, _, _ = m.get_state()
-        if args.tetra_mixed:
+        if args.tetra_solver == 1:
+            restore()
+            tq, itsq = timed(step_kwargs(args, solver=11), "rpsqmr")
+            qmr = {"value": steps / tq, "unit": "steps/s", "ms_per_step": tq / steps * 1e3,
+                   "iterations_per_step": itsq}
+        if args.tetra_mixed or args.tetra_solver == 1:
             restore()
             m.set_precision(pg.capi.PM_FP32C_REFINE)
             m.step(**kw)  # one-off set-up of the mode (copies, record layout, autotuner)
             restore()
-            tc, itsc = timed()
+            tc, itsc = timed(kw, sname + " compensated")
             uc, _, _ = m.get_state()
             du = float(np.abs(uc[:, :3] - u64[:, :3]).max() / np.abs(u64[:, :3]).max())
             dp_ = float(np.abs(uc[:, 3] - u64[:, 3]).max() / np.abs(u64[:, 3]).max())
@@ -646,24 +660,29 @@ def tetra_leg(args, steps, warmup):
     m.close()
     out = {"value": steps / t64, "unit": "steps/s", "steps": steps, "warmup": warmup,
            "ms_per_step": t64 / steps * 1e3,
-           "workload": "tetra10 Kuhn %d^3 on 2x2x1 m, %d equations, nad %d, rpsqmr tol %g, "
-                       "K re-assembled every step" % (args.tetra_n, neq, nad, kw["solvtol"]),
+           "workload": "tetra10 Kuhn %d^3 on 2x2x1 m, %d equations, nad %d, %s tol %g, "
+                       "K re-assembled every step" % (args.tetra_n, neq, nad, sname,
+                                                      kw["solvtol"]),
            "iterations_per_step": its64, "clocks": clk.summary()}
     if mixed:
         out["fp32_refine"] = mixed
+    if qmr:
+        out["rpsqmr_fp64"] = qmr
     return out
 
 
 def run_tetra(args):
     t = tetra_leg(args, args.steps, args.warmup)
-    out = {"metric": "Biot steps/s, unstructured tetra10 rpsqmr: FP64 plain vs FP32+refine",
+    out = {"metric": "Biot steps/s, unstructured tetra10 %s: FP64 plain vs FP32+refine"
+                     % {1: "pcg", 11: "rpsqmr"}[args.tetra_solver],
            "value": t["value"], "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t["ms_per_step"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded jitter, two layers, point source)",
            "config": {"workload": t["workload"],
                       "iterations_per_step": t["iterations_per_step"]},
-           "fp32_refine": t.get("fp32_refine"), "clocks": t["clocks"]}
+           "fp32_refine": t.get("fp32_refine"), "rpsqmr_fp64": t.get("rpsqmr_fp64"),
+           "clocks": t["clocks"]}
     print(json.dumps(out), flush=True)
 
 

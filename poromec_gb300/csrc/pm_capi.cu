@@ -569,7 +569,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
     } else {
       // The compensated products (2^-32 per value) make the recursive
       // residual drift from b - A x.  Every time it has fallen by a factor
-      // kDrop (in (r, m r)) since the last replacement, and when it meets
+      // drop (in (r, m r)) since the last replacement, and when it meets
       // pcg's test, it is replaced by the FP64 residual of the current x;
       // the iteration then goes on with the same search direction until the
       // replaced residual itself meets the test (the refinement of the FP64
@@ -579,7 +579,8 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       // can on small systems whose Krylov space is exhausted), the remaining
       // correction is solved by restarted sweeps with the FP64 operator,
       // A dx = b - A x to the same absolute target, x += dx.
-      constexpr double kDrop = 1e-4;
+      double drop = 1e-4;  // PM_RR_DROP overrides (a tuning knob)
+      if (const char* e = std::getenv("PM_RR_DROP")) drop = std::atof(e);
       constexpr int kMaxReplace = 256, kMaxSweeps = 8;
       double d_ref = -1.0;
       bool restart = false;
@@ -594,7 +595,7 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
           break;
         }
         const bool met = ks.conv_flag == 1;
-        if (!met && std::fabs(ks.d) > kDrop * d_ref) continue;
+        if (!met && std::fabs(ks.d) > drop * d_ref) continue;
         h->launches += 2;
         PM_CUDA(pm::spmv(P, val64, V.x, h->D.dx, 0, nullptr, nullptr, nullptr, h->stream));
         PM_CUDA(pm::pcgc_replace(n, d_b, h->D.dx, h->D.m, V, h->D.ks, h->D.partial,
