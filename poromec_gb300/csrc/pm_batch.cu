@@ -140,11 +140,12 @@ __global__ void __launch_bounds__(256)
   const int inst = seg_range(B, e0, e1);
   if (B.done[inst]) return;
   const double alpha = B.bs[inst].alpha;
+  // x, r and q streamed (evict-first): L2 keeps p (or its pair), m and z
   double acc = 0.0;
   for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
-    x[i] = x[i] + alpha * p[i];
-    const double ri = r[i] - alpha * q[i];
-    r[i] = ri;
+    __stcs(&x[i], __ldcs(&x[i]) + alpha * p[i]);
+    const double ri = __ldcs(&r[i]) - alpha * __ldcs(&q[i]);
+    __stcs(&r[i], ri);
     const double zi = ri * m[i];
     z[i] = zi;
     acc += ri * zi;
@@ -175,7 +176,7 @@ __global__ void __launch_bounds__(256)
   if (B.done[inst]) return;
   const double beta = B.bs[inst].beta;
   for (int i = e0 + threadIdx.x; i < e1; i += blockDim.x) {
-    const double pi = z[i] + beta * p[i];
+    const double pi = __ldcs(&z[i]) + beta * p[i];
     p[i] = pi;
     if (pair) pair_store(pi, pair, i);
   }

@@ -187,11 +187,13 @@ __global__ void __launch_bounds__(256)
     if (blockIdx.x == 0 && threadIdx.x == 0) ks->conv_flag = 3;
     return;
   }
+  // x, r and q are streamed (evict-first), so that L2 keeps the operand of
+  // the next product (p, or its FP32 pair), m and z
   double acc = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    x[i] = x[i] + alpha * p[i];
-    const double ri = r[i] - alpha * q[i];
-    r[i] = ri;
+    __stcs(&x[i], __ldcs(&x[i]) + alpha * p[i]);
+    const double ri = __ldcs(&r[i]) - alpha * __ldcs(&q[i]);
+    __stcs(&r[i], ri);
     const double zi = ri * m[i];
     z[i] = zi;
     acc += ri * zi;
@@ -214,7 +216,7 @@ __global__ void __launch_bounds__(256)
   if (krylov_skip(ks, false)) return;
   const double beta = ks->beta;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+    p[i] = __ldcs(&z[i]) + beta * p[i];  // p stays in L2 for the product
 }
 
 // ---- mixed-precision PCG (inner solve of the FP64 refinement) ----------------
@@ -674,7 +676,7 @@ __global__ void __launch_bounds__(256, MINB)
     if ((t & (o2 - 1)) == 0 && r < d) {
       const double v = double(k.s) + double(k.c);
       y[e0 + r] = v;
-      if (MODE != 0) dsum += v * xd[e0 + r];
+      if (MODE != 0) dsum += v * __ldcs(&xd[e0 + r]);
     }
   }
   if (MODE != 0) {
@@ -1202,9 +1204,9 @@ __global__ void __launch_bounds__(256)
   if (krylov_skip(ks, false)) return;
   const double beta = ks->beta;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const double pi = z[i] + beta * p[i];
-    p[i] = pi;
-    split_store(pi, pc, i);
+    const double pi = __ldcs(&z[i]) + beta * __ldcs(&p[i]);
+    __stcs(&p[i], pi);
+    split_store(pi, pc, i);  // the product's operand: kept in L2
   }
 }
 
