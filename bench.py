@@ -85,6 +85,9 @@ def parse(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="one step of the same workload only (for the ncu launch list)")
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="with --profile: then a solve of this many PCG iterations between "
+                         "cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--workload", default="cube",
                     choices=["cube", "batched", "adjoint", "tetra"],
                     help="batched: only the batch of independent cubes; adjoint: the "
@@ -769,8 +772,22 @@ def run_gpu(args):
             m.set_precision(pg.capi.PM_FP32C_REFINE)
         info = m.step(**step_kw)
         torch.cuda.synchronize()
-        print(json.dumps({"profile_step": True, "pcg_iterations": int(m.timers()[4]),
-                          "nlit": info.nlit, "kernels": int(m.timers()[7])}), flush=True)
+        out = {"profile_step": True, "pcg_iterations": int(m.timers()[4]),
+               "nlit": info.nlit, "kernels": int(m.timers()[7])}
+        if args.profile_iters:
+            # a solve of exactly --profile-iters iterations on the step's matrix
+            # (tolerance 0, ended by maxit) between cudaProfilerStart/Stop: the
+            # in-loop kernels alone for `ncu --profile-from-start off`
+            b = np.random.default_rng(1).standard_normal(m.neq)
+            torch.cuda.profiler.start()
+            try:
+                m.solve(b, solver=1, precond=2, tol=0.0, maxit=args.profile_iters)
+            except pg.PMError:
+                pass
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
+            out["profiled_iterations"] = args.profile_iters
+        print(json.dumps(out), flush=True)
         return
     warm_iters = []
     for _ in range(args.warmup):
