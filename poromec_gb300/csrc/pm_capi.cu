@@ -1129,6 +1129,7 @@ int batch_setup(Handle* h) {
   PM_TRY(up(&B.counter, (unsigned*)nullptr, (size_t)ni));
   PM_TRY(up(&h->P.node_inst, h->h_inst_act.data(), h->h_inst_act.size()));
   h->P.inst_done = B.done;
+  PM_TRY(pm::build_meta(h, h->h_inst_act.data()));
   PM_TRY(up(&h->d_insweep, (int*)nullptr, (size_t)ni));
   PM_TRY(up(&h->d_conv0, (double*)nullptr, (size_t)ni));
   PM_TRY(up(&h->d_bnorms, (double*)nullptr, (size_t)2 * ni));
@@ -1366,7 +1367,7 @@ void free_all(Handle* h) {
                   D.norms, D.err, P.eq0, P.d, P.W, P.low, P.val_off, P.col_off, P.cols, P.val,
                   P.val32, P.valh, P.vall, P.rec, P.rec_off, P.node_val_off, P.node_W,
                   P.order, P.cs_desc, P.cs_batch_slot, P.cs_batch_off, P.cs_batch_bytes,
-                  P.cs_cta_batch, P.fault};
+                  P.cs_cta_batch, P.fault, P.meta};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)D.kv32.p, (void*)D.kv32.q, (void*)D.kv32.c})

@@ -63,12 +63,14 @@ struct Panels {
   // indexed by node id - 1
   int64_t* node_val_off = nullptr;
   int32_t* node_W = nullptr;
+  int4* meta = nullptr;  // per visiting slot (PanelView::meta), or null
   PanelView view() const {
-    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols, nullptr, nullptr};
+    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols, nullptr, nullptr, meta};
   }
   // the view of the batched iteration: rows of converged instances skipped
   PanelView bview() const {
-    return PanelView{nact, order, eq0, d, W, low, val_off, col_off, cols, node_inst, inst_done};
+    return PanelView{nact,   order,    eq0,  d,         W,        low,
+                     val_off, col_off, cols, node_inst, inst_done, meta};
   }
   CompVals comp(int shape) const {
     return CompVals{valh,          vall,          rec,          rec_off,        rec_max,
@@ -235,5 +237,8 @@ struct Handle {
 int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
                     const int32_t* fnno, const double* x, const int32_t* num);
 int build_rec_layout(Handle* h);
+// PanelView::meta from the host panel arrays (inst: the instance of each
+// active node, or null for one mesh); leaves it null when a field does not fit
+int build_meta(Handle* h, const int32_t* inst);
 
 }  // namespace pm

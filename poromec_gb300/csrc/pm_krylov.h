@@ -57,7 +57,50 @@ struct PanelView {
   // for a single mesh
   const int32_t* node_inst;
   const int* inst_done;
+  // the same per visiting slot as one 16-byte record, so that a node's panel
+  // is located by one load: x eq0, y d | W << 3 | instance << 16,
+  // z val_off, w col_off (unsigned); null when a field does not fit
+  // (W >= 8192, 65536 instances or more, 2^32 panel values or columns)
+  const int4* meta;
 };
+
+// A node's panel located from its visiting slot: meta record or the separate
+// arrays; on = false past the last slot or for a converged instance.
+struct NodeRef {
+  int e0, d, W;
+  int64_t vo, co;
+  bool on;
+};
+// the node of a meta record m already loaded for slot
+__device__ __forceinline__ NodeRef node_from_meta(const PanelView& P, const int4& m, int slot) {
+  NodeRef r{0, 0, 0, 0, 0, false};
+  if (slot >= P.nact) return r;
+  if (P.inst_done && P.inst_done[(unsigned)m.y >> 16]) return r;
+  r.e0 = m.x;
+  r.d = m.y & 7;
+  r.W = (m.y >> 3) & 8191;
+  r.vo = (int64_t)(unsigned)m.z;
+  r.co = (int64_t)(unsigned)m.w;
+  r.on = true;
+  return r;
+}
+__device__ __forceinline__ NodeRef node_ref(const PanelView& P, int slot) {
+  NodeRef r{0, 0, 0, 0, 0, false};
+  if (slot >= P.nact) return r;
+  if (P.meta) {
+    return node_from_meta(P, P.meta[slot], slot);
+  } else {
+    const int node = P.order[slot];
+    if (P.inst_done && P.inst_done[P.node_inst[node]]) return r;
+    r.e0 = P.eq0[node];
+    r.d = P.d[node];
+    r.W = P.W[node];
+    r.vo = P.val_off[node];
+    r.co = P.col_off[node];
+  }
+  r.on = true;
+  return r;
+}
 
 // Scalars of one Krylov solve, kept in device memory so that a captured
 // graph of iterations runs without host round trips.

@@ -286,7 +286,27 @@ int build_structure(Handle* h, const int32_t* ix, const int32_t* idflag,
   if ((st = upload(h, &h->D.dofkind, kind.data(), kind.size()))) return st;
   if ((st = upload(h, &h->D.fnno, fnno, (size_t)nnode))) return st;
   h->h_fnno.assign(fnno, fnno + nnode);
-  return PM_OK;
+  return build_meta(h, nullptr);
+}
+
+int build_meta(Handle* h, const int32_t* inst) {
+  Panels& P = h->P;
+  if (P.meta) {
+    cudaFree(P.meta);
+    P.meta = nullptr;
+  }
+  const int nact = P.nact;
+  if (nact == 0 || P.nnz >= (int64_t(1) << 32) || P.ncols >= (int64_t(1) << 32)) return PM_OK;
+  std::vector<int4> m(nact);
+  for (int s = 0; s < nact; ++s) {
+    const int k = h->h_order[s];
+    const int W = h->h_W[k], d = h->h_d[k], in = inst ? inst[k] : 0;
+    if (W >= 8192 || d > 7 || in >= 65536) return PM_OK;
+    const uint32_t dw = (uint32_t)d | ((uint32_t)W << 3) | ((uint32_t)in << 16);
+    m[s] = make_int4(h->h_eq0[k], (int)dw, (int)(uint32_t)h->h_val_off[k],
+                     (int)(uint32_t)h->h_col_off[k]);
+  }
+  return upload(h, &P.meta, m.data(), (size_t)nact);
 }
 
 // Offsets of the node records of the compensated operator (layout in

@@ -81,16 +81,15 @@ __global__ void __launch_bounds__(256)
   constexpr int kNodesPerWarp = 32 / kSub;
   double dsum = 0.0;
   for (int base = warp * kNodesPerWarp; base < P.nact; base += nwarp * kNodesPerWarp) {
-    const int slot = base + (lane >> 3);
-    const int node = slot < P.nact ? P.order[slot] : 0;
+    const NodeRef nr = node_ref(P, base + (lane >> 3));
     int e0 = 0, d = 0, W = 0;
     T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
-    if (slot < P.nact && !(P.inst_done && P.inst_done[P.node_inst[node]])) {
-      e0 = P.eq0[node];
-      d = P.d[node];
-      W = P.W[node];
-      const T* v = val + P.val_off[node];
-      const int32_t* cols = P.cols + P.col_off[node];
+    if (nr.on) {
+      e0 = nr.e0;
+      d = nr.d;
+      W = nr.W;
+      const T* v = val + nr.vo;
+      const int32_t* cols = P.cols + nr.co;
       if (d == 4) {
         for (int c = t; c < W; c += kSub) {
           const T xv = x[cols[c]];
@@ -642,20 +641,19 @@ __global__ void __launch_bounds__(256, MINB)
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarp = (int)((gridDim.x * blockDim.x) >> 5);
   constexpr int kNodesPerWarp = 32 / S;
+  const int stride = nwarp * kNodesPerWarp;
   double dsum = 0.0;
-  for (int base = warp * kNodesPerWarp; base < P.nact; base += nwarp * kNodesPerWarp) {
-    const int slot = base + lane / S;
-    const int node = slot < P.nact ? P.order[slot] : 0;
+  for (int base = warp * kNodesPerWarp; base < P.nact; base += stride) {
+    const NodeRef nr = node_ref(P, base + lane / S);
     int e0 = 0, d = 0, W = 0;
     F2 a[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    if (slot < P.nact && !(P.inst_done && P.inst_done[P.node_inst[node]])) {
-      e0 = P.eq0[node];
-      d = P.d[node];
-      W = P.W[node];
-      const int64_t vo = P.val_off[node];
-      const float* h = vh + vo;
-      const int8_t* l = vl + vo;
-      const int32_t* cols = P.cols + P.col_off[node];
+    if (nr.on) {
+      e0 = nr.e0;
+      d = nr.d;
+      W = nr.W;
+      const float* h = vh + nr.vo;
+      const int8_t* l = vl + nr.vo;
+      const int32_t* cols = P.cols + nr.co;
       if (d == 4) cf_rows<4, S, U, PK>(h, l, cols, xp, W, t, a);
       else if (d == 3) cf_rows<3, S, U, PK>(h, l, cols, xp, W, t, a);
       else if (d == 2) cf_rows<2, S, U, PK>(h, l, cols, xp, W, t, a);
