@@ -152,30 +152,42 @@ def _steps(pb, precision, host_loop, steps, **kw):
             os.environ["PM_BATCH_HOST_STEP"] = old
 
 
-@pytest.mark.parametrize("precision", [pg.capi.PM_FP64, pg.capi.PM_FP32C_REFINE])
-def test_batch_step_graph_matches_host_loop(instances, precision, monkeypatch):
+@pytest.mark.parametrize("precision,stop_crit", [(pg.capi.PM_FP64, 1),
+                                                  (pg.capi.PM_FP32C_REFINE, 1),
+                                                  (pg.capi.PM_FP64, 2)])
+def test_batch_step_graph_matches_host_loop(instances, precision, stop_crit, monkeypatch):
     """The batch step as one CUDA graph (conditional nodes for the nonlinear
     loop, the refinement sweeps and the PCG iterations, decided on the
     device) runs the host loop's kernels in the host loop's order: the same
     state bit for bit, the same per-instance iterations and nonlinear
-    counts.  The compensated SpMV shape is fixed so both handles run the same
-    kernel (the autotuner times kernels)."""
+    counts, under both stop tests of cal_residuo_pm (with stop_crit 2 some of
+    these instances stop at the nonlinear limit within a few steps, as they do
+    on the oracle: both drivers fail the same step with the same status).
+    The compensated SpMV shape is fixed so both handles run the same kernel
+    (the autotuner times kernels)."""
     monkeypatch.setenv("PM_SPMV_SHAPE", "314")
     pb = meshgen.union_problem(instances)
-    kw = dict(maxnlit=500, tol=1e-4, stop_crit=1, solver=1, precond=2, solvtol=1e-11,
+    kw = dict(maxnlit=500, tol=1e-4, stop_crit=stop_crit, solver=1, precond=2, solvtol=1e-11,
               maxit=100000)
     ug, og = _steps(pb, precision, False, 4, **kw)
     uh, oh = _steps(pb, precision, True, 4, **kw)
     for a, b in zip(ug, uh):
         assert np.array_equal(a, b)
-    graph_steps = 0
-    for (gl, gi, gr, (git, gnl), gt), (hl, hi, hr, (hit, hnl), ht) in zip(og, oh):
+    assert len(og) == len(oh)
+    graph_steps = done = 0
+    for g, h in zip(og, oh):
+        if len(g) == 2 or len(h) == 2:  # a failed step: the same status and message
+            assert g == h
+            continue
+        (gl, gi, gr, (git, gnl), gt), (hl, hi, hr, (hit, hnl), ht) = g, h
         assert (gl, gi, gr) == (hl, hi, hr)
         assert np.array_equal(git, hit) and np.array_equal(gnl, hnl)
         assert ht[0] > 0.0  # the host loop times its phases
         graph_steps += gt[0] == 0.0 and gt[3] > 0.0  # the graph: one time for the step
+        done += 1
     # the compensated handle's first step tunes and splits on the host loop
-    assert graph_steps >= 3
+    assert done >= 1
+    assert graph_steps == done - (precision == pg.capi.PM_FP32C_REFINE)
 
 
 @pytest.mark.parametrize("case", ["maxnlit", "maxit"])
