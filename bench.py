@@ -894,6 +894,8 @@ def run_gpu(args):
             for _ in range(args.steps):
                 info = m.step(**dict(step_kw, maxit=budget))
                 mi.append((int(m.timers()[4]), info.refine, info.nlit))
+                log("mode %d timed step %d: %d PCG iterations, %d replacements, nlit %d"
+                    % (mode, len(mi), mi[-1][0], info.refine, info.nlit))
             barrier()
             t_mixed = time.perf_counter() - t0
             um, _, _ = m.get_state()

@@ -578,24 +578,33 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
       // residual misses the test there (or the recurrence breaks down, as it
       // can on small systems whose Krylov space is exhausted), the remaining
       // correction is solved by restarted sweeps with the FP64 operator,
-      // A dx = b - A x to the same absolute target, x += dx.
+      // A dx = b - A x to the same absolute target, x += dx.  The same
+      // sweeps take over when the compensated iteration stalls: a
+      // replacement is also made after kForce iterations without one, and
+      // when the replaced (r, m r) has not fallen below kProgress times its
+      // value at the previous replacement, the compensated operator has
+      // reached its own error level (|A| |x| large against |b|: the small
+      // increments late in a load history), so the iteration stops there.
       double drop = 1e-4;  // PM_RR_DROP overrides (a tuning knob)
       if (const char* e = std::getenv("PM_RR_DROP")) drop = std::atof(e);
-      constexpr int kMaxReplace = 256, kMaxSweeps = 8;
-      double d_ref = -1.0;
+      constexpr int kMaxReplace = 256, kMaxSweeps = 8, kForce = 1024;
+      constexpr double kProgress = 0.5;
+      double d_ref = -1.0, d_true = -1.0;
+      int it_ref = 0;
       bool restart = false;
       for (;;) {
         PM_CUDA(cudaGraphLaunch(*g, h->stream));
         h->launches += 3 * kGraphIters;
         PM_TRY(read_scalars(h, &ks));
-        if (d_ref < 0.0) d_ref = std::fabs(ks.bmb);
+        if (d_ref < 0.0) d_ref = d_true = std::fabs(ks.bmb);
         if (ks.conv_flag == 2) break;
         if (ks.conv_flag == 3) {  // x holds the last finite iterate
           restart = d_x != V.x;
           break;
         }
         const bool met = ks.conv_flag == 1;
-        if (!met && std::fabs(ks.d) > drop * d_ref) continue;
+        const bool force = ks.iter - it_ref >= kForce;
+        if (!met && !force && std::fabs(ks.d) > drop * d_ref) continue;
         h->launches += 2;
         PM_CUDA(pm::spmv(P, val64, V.x, h->D.dx, 0, nullptr, nullptr, nullptr, h->stream));
         PM_CUDA(pm::pcgc_replace(n, d_b, h->D.dx, h->D.m, V, h->D.ks, h->D.partial,
@@ -606,8 +615,13 @@ int krylov(Handle* h, int solver, const double* d_b, double* d_x, double tol, in
           fprintf(stderr, "residual replacement %d after %d its: sqrt|(r, m r)| %.3e target %.3e\n",
                   sweeps, ks.iter, std::sqrt(std::fabs(ks.d)), ks.conv);
         d_ref = std::fabs(ks.d);
+        it_ref = ks.iter;
         if (ks.conv_flag != 0) break;
-        if (met || sweeps >= kMaxReplace) {
+        const bool stalled = d_ref > kProgress * d_true;
+        d_true = d_ref;
+        if (met || stalled || sweeps >= kMaxReplace) {
+          if (h->debug && stalled && !met)
+            fprintf(stderr, "compensated iteration stalled: FP64 correction sweeps\n");
           restart = d_x != V.x;
           if (!restart) ks.conv_flag = 2;
           break;
