@@ -97,3 +97,69 @@ def test_oracle_flop_count(nen):
         assert 1.8e6 < f < 1.95e6
     else:
         assert 2e4 < f < 5e4
+
+
+def _fortran_bindings(text):
+    """name -> [(arg, passed by value)] for every ISO_C_BINDING interface in
+    the integration guide's Fortran module."""
+    lines, out, cur = [], {}, None
+    for raw in text.splitlines():
+        line = raw.split("!")[0].rstrip()
+        if lines and lines[-1].endswith("&"):
+            lines[-1] = lines[-1][:-1] + " " + line.strip()
+        else:
+            lines.append(line)
+    for line in lines:
+        m = re.search(r"(?:function|subroutine)\s+(\w+)\s*\(([^)]*)\)\s*bind\(c,\s*name='(\w+)'\)",
+                      line)
+        if m:
+            args = [a.strip() for a in m.group(2).split(",") if a.strip()]
+            cur = (m.group(3), args, {})
+            out[m.group(3)] = cur
+            continue
+        if cur and re.match(r"\s*end\s+(function|subroutine)", line):
+            cur = None
+            continue
+        if cur and "::" in line:
+            typ, names = line.split("::", 1)
+            for nm in names.split(","):
+                nm = nm.strip().split("(")[0]
+                if nm:
+                    cur[2][nm] = ("value" in typ, "c_ptr" in typ)
+    return {k: [(a,) + decl[a] for a in args] for k, (_, args, decl) in out.items()}
+
+
+def _c_prototypes(text):
+    """name -> [param declaration] for every pm_* prototype of the header."""
+    flat = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(pm_\w+)\s*\(([^;{]*?)\)\s*;", flat, flags=re.S):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(1)] = params
+    return out
+
+
+def test_fortran_bindings_match_the_header():
+    """The Fortran ISO_C_BINDING module that the integration guide gives the
+    reference's maintainers binds only functions the header declares, with
+    the header's argument count, and passes each argument the way the C
+    parameter takes it: numbers by value, arrays, strings and handle outputs
+    by reference, and a type(c_ptr) by value only where C takes a pointer or
+    an opaque handle (a nullable array is passed as c_loc(a) or c_null_ptr)."""
+    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    header = open(os.path.join(ROOT, "include", "poromec_gb300.h")).read()
+    binds, protos = _fortran_bindings(guide), _c_prototypes(header)
+    assert len(binds) >= 20
+    for name, args in binds.items():
+        assert name in protos, name
+        params = protos[name]
+        assert len(args) == len(params), (name, args, params)
+        for (arg, by_value, is_cptr), p in zip(args, params):
+            c_pointer = "*" in p
+            handle = p.startswith(("pm_handle", "pm_deck"))
+            if not by_value:
+                assert c_pointer, (name, arg, p)
+            elif is_cptr:
+                assert c_pointer or handle, (name, arg, p)
+            else:
+                assert not c_pointer and not handle, (name, arg, p)
