@@ -163,3 +163,31 @@ def test_fortran_bindings_match_the_header():
                 assert c_pointer or handle, (name, arg, p)
             else:
                 assert not c_pointer and not handle, (name, arg, p)
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every argtypes list that the Python mirror (poromec_gb300/capi.py)
+    declares has the header's length, and pointers, handles, ints and
+    doubles in the header's places: a drifted signature would pass
+    arguments in the wrong registers without any error."""
+    from poromec_gb300 import capi
+    lib = capi.load()
+    protos = _c_prototypes(open(os.path.join(ROOT, "include", "poromec_gb300.h")).read())
+    pointer_types = (ctypes.c_void_p, ctypes.c_char_p)
+    checked = 0
+    for name, params in protos.items():
+        argtypes = getattr(lib, name).argtypes
+        if argtypes is None:
+            continue
+        assert len(argtypes) == len(params), (name, argtypes, params)
+        for a, p in zip(argtypes, params):
+            if "*" in p or p.startswith(("pm_handle", "pm_deck")):
+                assert a in pointer_types or issubclass(a, ctypes._Pointer), (name, p, a)
+            elif p.startswith(("int ", "int32_t ")):
+                assert a is ctypes.c_int, (name, p, a)
+            elif p.startswith("double "):
+                assert a is ctypes.c_double, (name, p, a)
+            else:
+                raise AssertionError((name, p, a))
+        checked += 1
+    assert checked >= 40
