@@ -690,7 +690,7 @@ def run_tetra(args):
 
 
 def column_leg(args, steps=20):
-    """BASELINE config 1, the reference's CPU-runnable case: the 2 x 2 x 40
+    """The reference's CPU-runnable case: the 2 x 2 x 40
     hexa20 consolidation column (4,032 equations before restraints), 1 MPa
     top load from t = 0, 20 implicit Euler steps of 10 s, diagonal PCG to
     1e-10, maxnlit 500, stop_crit 1.  The GPU runs the 20 steps once untimed
